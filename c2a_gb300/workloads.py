@@ -1,0 +1,216 @@
+"""Seeded CCD query workloads (the benchmark configurations, synthetic).
+
+A workload is a list of meshes plus, per query, the two model indices, the
+two seed triangles (C2A's initial upper-bound pair, ``dres.last_triA/B``) and
+the four poses of C2A_Solve: begin/end of object A, begin/end of object B
+(C2A/C2A.h:23-35).  Object A stays at the identity; object B starts at a
+random orientation with a surface gap of ``s * diag``, translates towards A
+inside a cone and rotates about a uniform axis: R1 = R0 * Rot(axis, |w|), so
+the reference's body-frame axis/angle recovers exactly that rotation
+(C2A/src/InterpMotion.cpp:228-270).
+
+The reference measures nothing, so these stand in for its scenes: the shapes,
+sizes and value ranges follow the benchmark configurations; the numbers are
+drawn from numpy's PCG64 with a fixed seed.
+
+Pose rows are 48 float64: R0a(9) T0a(3) R1a(9) T1a(3) R0b(9) T0b(3) R1b(9) T1b(3),
+matrices row-major.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .meshes import Mesh, torus_knot, icosphere, triangle_soup
+
+POSE_WIDTH = 48
+
+
+@dataclass
+class Workload:
+    name: str
+    meshes: list
+    qint: np.ndarray        # (n, 4) int32: model_a, model_b, seed_a, seed_b
+    poses: np.ndarray       # (n, 48) float64
+    params: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.qint.shape[0])
+
+    def subset(self, idx) -> "Workload":
+        idx = np.asarray(idx)
+        return Workload(self.name, self.meshes, np.ascontiguousarray(self.qint[idx]),
+                        np.ascontiguousarray(self.poses[idx]), dict(self.params))
+
+
+def random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """(n, 3, 3) uniformly distributed rotations (normalised Gaussian quaternions)."""
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    return quat_to_mat(q)
+
+
+def quat_to_mat(q: np.ndarray) -> np.ndarray:
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    R = np.empty((len(q), 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - w * z)
+    R[:, 0, 2] = 2 * (x * z + w * y)
+    R[:, 1, 0] = 2 * (x * y + w * z)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - w * x)
+    R[:, 2, 0] = 2 * (x * z - w * y)
+    R[:, 2, 1] = 2 * (y * z + w * x)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def axis_angle(axis: np.ndarray, ang: np.ndarray) -> np.ndarray:
+    """(n, 3, 3) rotations about unit ``axis`` by ``ang`` (Rodrigues)."""
+    half = 0.5 * ang
+    q = np.concatenate([axis * np.sin(half)[:, None], np.cos(half)[:, None]], axis=1)
+    return quat_to_mat(q)
+
+
+def unit_vectors(rng: np.random.Generator, n: int) -> np.ndarray:
+    v = rng.standard_normal((n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def cone_directions(rng: np.random.Generator, centre: np.ndarray, half_angle: float) -> np.ndarray:
+    """Unit vectors uniform in the cone of ``half_angle`` around each row of ``centre``."""
+    n = len(centre)
+    cos_t = 1.0 - rng.uniform(0, 1, n) * (1.0 - np.cos(half_angle))
+    sin_t = np.sqrt(np.maximum(0.0, 1.0 - cos_t * cos_t))
+    phi = rng.uniform(0, 2 * np.pi, n)
+    a = np.where(np.abs(centre[:, :1]) < 0.9, np.array([[1.0, 0, 0]]), np.array([[0, 1.0, 0]]))
+    e1 = np.cross(centre, a)
+    e1 /= np.linalg.norm(e1, axis=1, keepdims=True)
+    e2 = np.cross(centre, e1)
+    return (cos_t[:, None] * centre + sin_t[:, None] * (np.cos(phi)[:, None] * e1 + np.sin(phi)[:, None] * e2))
+
+
+def _subsample(points: np.ndarray, k: int) -> np.ndarray:
+    if len(points) <= k:
+        return points
+    idx = np.linspace(0, len(points) - 1, k).astype(np.int64)
+    return points[idx]
+
+
+def place_at_gap(mesh_a: Mesh, mesh_b: Mesh, R0: np.ndarray, u: np.ndarray, gap: np.ndarray,
+                 skeleton_points: int = 128, device: str | None = None) -> np.ndarray:
+    """Translations T0 putting B (rotated by R0) along direction u from A's
+    centroid so that the skeleton estimate of the surface gap equals ``gap``
+    (outermost crossing: coarse scan inwards, then bisection)."""
+    import torch
+
+    dev = device or ("cuda" if torch.cuda.is_available() else "cpu")
+    sa = torch.as_tensor(_subsample(mesh_a.skeleton, skeleton_points), dtype=torch.float64, device=dev)
+    sb = torch.as_tensor(_subsample(mesh_b.skeleton, skeleton_points), dtype=torch.float64, device=dev)
+    ca = torch.as_tensor(mesh_a.verts.mean(axis=0), dtype=torch.float64, device=dev)
+    cb = torch.as_tensor(mesh_b.verts.mean(axis=0), dtype=torch.float64, device=dev)
+    rr = mesh_a.skeleton_radius + mesh_b.skeleton_radius
+    n = len(u)
+    out = np.empty((n, 3))
+    chunk = 4096 if dev == "cuda" else 512
+    dmax = mesh_a.bbox_diag() + mesh_b.bbox_diag() + float(np.max(gap)) + 1.0
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        Rt = torch.as_tensor(R0[s:e], dtype=torch.float64, device=dev)
+        ut = torch.as_tensor(u[s:e], dtype=torch.float64, device=dev)
+        gt = torch.as_tensor(gap[s:e], dtype=torch.float64, device=dev)
+        bl = torch.einsum("nij,kj->nki", Rt, sb - cb)  # B skeleton about its centroid, rotated
+
+        def g(D):
+            pts = bl + (ca + ut * D[:, None])[:, None, :]
+            d = torch.cdist(pts, sa.unsqueeze(0).expand(len(pts), -1, -1))
+            return d.flatten(1).min(dim=1).values - rr
+
+        hi = torch.full((e - s,), dmax, dtype=torch.float64, device=dev)
+        lo = torch.zeros_like(hi)
+        found = torch.zeros(e - s, dtype=torch.bool, device=dev)
+        steps = 48
+        for k in range(1, steps + 1):
+            D = torch.full_like(hi, dmax * (1.0 - k / steps))
+            below = (g(D) < gt) & ~found
+            lo = torch.where(below, D, lo)
+            hi = torch.where(below, D + dmax / steps, hi)
+            found |= below
+        for _ in range(30):
+            mid = 0.5 * (lo + hi)
+            below = g(mid) < gt
+            lo = torch.where(below, mid, lo)
+            hi = torch.where(below, hi, mid)
+        D = hi
+        T = (ca + ut * D[:, None]) - torch.einsum("nij,j->ni", Rt, cb)
+        out[s:e] = T.cpu().numpy()
+    return out
+
+
+def ccd_queries(mesh_a: Mesh, mesh_b: Mesh, n: int, seed: int, gap_range=(0.05, 1.0), speed_range=(0.5, 3.0),
+                speed_log=False, cone_deg: float = 30.0, max_rot: float = np.pi, device: str | None = None,
+                model_a: int = 0, model_b: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    """``n`` queries of the benchmark family: returns (qint (n, 4), poses (n, 48))."""
+    rng = np.random.default_rng(seed)
+    diag = mesh_a.bbox_diag()
+    R0b = random_rotations(rng, n)
+    u = unit_vectors(rng, n)
+    gap = rng.uniform(gap_range[0], gap_range[1], n) * diag
+    if speed_log:
+        speed = np.exp(rng.uniform(np.log(speed_range[0]), np.log(speed_range[1]), n)) * diag
+    else:
+        speed = rng.uniform(speed_range[0], speed_range[1], n) * diag
+    vdir = cone_directions(rng, -u, np.deg2rad(cone_deg))
+    axis = unit_vectors(rng, n)
+    ang = rng.uniform(0.0, max_rot, n)
+    T0b = place_at_gap(mesh_a, mesh_b, R0b, u, gap, device=device)
+    T1b = T0b + speed[:, None] * vdir
+    R1b = np.einsum("nij,njk->nik", R0b, axis_angle(axis, ang))
+    poses = np.zeros((n, POSE_WIDTH))
+    eye = np.eye(3).reshape(9)
+    poses[:, 0:9] = eye
+    poses[:, 12:21] = eye
+    poses[:, 24:33] = R0b.reshape(n, 9)
+    poses[:, 33:36] = T0b
+    poses[:, 36:45] = R1b.reshape(n, 9)
+    poses[:, 45:48] = T1b
+    qint = np.zeros((n, 4), dtype=np.int32)
+    qint[:, 0] = model_a
+    qint[:, 1] = model_b
+    return qint, poses
+
+
+def default_params(diag: float, th_ca_rel: float, qsize: int) -> dict:
+    """Harness mapping of C2A_Solve's constants: th_ca -> tolerance_d and
+    m_toc_delta (C2A_Solve ignores th_ca, C2A/src/C2A.cpp:2326, 2384-2388);
+    t_delta 1e-4; contact threshold 2 d + 0.001 (C2A.cpp:2433); 150 CA
+    iterations (C2A.cpp:2079).  qsize is the GPU front capacity."""
+    th_ca = th_ca_rel * diag
+    return dict(tol_d=th_ca, tol_t=1e-4, toc_delta=th_ca, contact_abs=0.001, with_contacts=1, max_iters=150,
+                qsize=qsize, th_ca=th_ca)
+
+
+def config1(n: int = 1000, seed: int = 1, device: str | None = None) -> Workload:
+    """Two (2,3) torus-knot tubes, 100 x 16 = 3,200 triangles each; 1,000
+    queries; gap U[0.05, 1] diag; |v| U[0.5, 3] diag; |w| U[0, pi];
+    th_ca = 1e-3 diag; qsize 40."""
+    knot = torus_knot(2, 3, 100, 16, 1.0, 0.15)
+    qint, poses = ccd_queries(knot, knot, n, seed, device=device, model_a=0, model_b=0)
+    return Workload("config1_torusknot3200_1000q", [knot], qint, poses, default_params(knot.bbox_diag(), 1e-3, 40))
+
+
+def config2(n: int = 65536, seed: int = 2, device: str | None = None) -> Workload:
+    """Same family at 400 x 50 = 40,000 triangles, 65,536 queries,
+    th_ca = 1e-4 diag, qsize 64."""
+    knot = torus_knot(2, 3, 400, 50, 1.0, 0.15)
+    qint, poses = ccd_queries(knot, knot, n, seed, device=device, model_a=0, model_b=0)
+    return Workload("config2_torusknot40000_65536q", [knot], qint, poses, default_params(knot.bbox_diag(), 1e-4, 64))
+
+
+def small_knots(n: int, seed: int, segments: int = 24, around: int = 6, device: str | None = None) -> Workload:
+    """A quick-to-check variant of config 1 (288-triangle knots) for unit tests."""
+    knot = torus_knot(2, 3, segments, around, 1.0, 0.15)
+    qint, poses = ccd_queries(knot, knot, n, seed, device=device, model_a=0, model_b=0)
+    return Workload(f"knot{knot.num_tris}_{n}q", [knot], qint, poses, default_params(knot.bbox_diag(), 1e-3, 40))
