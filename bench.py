@@ -1,0 +1,339 @@
+#!/usr/bin/env python
+"""CCD queries per second of the GB300 C2A conservative-advancement path.
+
+Workload (one step = one batch): 65,536 seeded CCD queries between two
+procedural (2,3) torus-knot tubes of 40,000 triangles each (400 x 50), object
+A fixed, object B starting at a random pose with a gap of U[0.05, 1] diag,
+translating U[0.5, 3] diag towards A inside a cone and turning by U[0, pi]
+about a random axis; th_ca = 1e-4 diag (tolerance_d and m_toc_delta),
+t_delta = 1e-4, contacts within 2 d + 0.001 enumerated at every TOC, the
+reference's traversal order and seeds (triangle 0 of each model).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: queries/s with the queries already in HBM (device entry point,
+CUDA events around the kernel on its stream, L2 flushed between steps).
+e2e: the same through c2a_solve_batch with host buffers (H2D of the queries,
+D2H of results and dense contacts inside the timed region).
+--impl reference: the CPU oracle port of the reference (bit-identical to
+the reference's own code) on all host cores, on a bounded sample.
+Under torchrun each rank runs its own replica batch (queries are independent).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import signal
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from c2a_gb300 import workloads  # noqa: E402
+from c2a_gb300.dist import env_rank  # noqa: E402
+
+METRIC = "CCD queries/s on 1 GB300: learned+batched vs plain GPU CA at equal TOC (≤1e-6 rel)"
+UNIT = "queries/s"
+NODE_BYTES = 208   # FP64 node fields a BV test reads (R, Tr, l, r, angularRadius, R_loc, first_child)
+TRI_BYTES = 144    # two triangles (9 doubles each) per triangle test
+CONTACT_SLOTS = 64
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--queries", type=int, default=65536)
+    p.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU-baseline sample (0: auto)")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (200 ms period)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="c2a_clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.send_signal(signal.SIGTERM)
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": float(max(power))}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def profile_traffic():
+    """DRAM bytes per query of the CA kernel from the committed ncu summary (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ca_kernel_config2.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(wl, sample: int, threads: int):
+    """The oracle port (the reference's algorithm, bit-identical) on host threads."""
+    from oracle.oracle import Port, build
+
+    build(ref=False)
+    port = Port()
+    models = port.models(wl.meshes)
+    sub = wl.subset(np.arange(min(sample, wl.n)))
+    t0 = time.perf_counter()
+    res, _ = port.solve_batch(models, sub.qint, sub.poses, sub.params, threads=threads,
+                              contacts_per_query=CONTACT_SLOTS)
+    dt = time.perf_counter() - t0
+    return sub.n / dt, dt, res
+
+
+def auto_sample(wl, threads: int, target_s: float = 12.0) -> int:
+    from oracle.oracle import Port, build
+
+    build(ref=False)
+    port = Port()
+    models = port.models(wl.meshes)
+    sub = wl.subset(np.arange(min(64, wl.n)))
+    t0 = time.perf_counter()
+    port.solve_batch(models, sub.qint, sub.poses, sub.params, threads=threads, contacts_per_query=CONTACT_SLOTS)
+    per_query_wall = (time.perf_counter() - t0) / sub.n
+    return int(np.clip(target_s / max(per_query_wall, 1e-9), 256, wl.n))
+
+
+def run_reference(args, rank, world):
+    """--impl reference: CPU oracle port of the reference on all host cores."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    wl = workloads.config2(n=args.queries, seed=2, device="cpu", subset=args.cpu_sample or 4096)
+    sample = args.cpu_sample or auto_sample(wl, threads, target_s=10.0)
+    sample = min(sample, wl.n)
+    rates, times = [], []
+    for _ in range(args.warmup):
+        cpu_baseline(wl, min(sample, 256), threads)
+    for _ in range(args.steps):
+        r, dt, _ = cpu_baseline(wl, sample, threads)
+        rates.append(r)
+        times.append(dt)
+    value = float(sample * len(times) / sum(times))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
+            "config": config_dict(wl, args, sample_only=sample),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"first {sample} of the {wl.n} config-2 queries per step"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(wl, args, sample_only=None):
+    return {"workload": wl.name, "queries": wl.n if sample_only is None else int(sample_only),
+            "triangles_per_model": wl.meshes[0].num_tris, "models": "two (2,3) torus-knot tubes, 400 x 50",
+            "th_ca": wl.params["th_ca"], "t_delta": wl.params["tol_t"], "qsize": wl.params["qsize"],
+            "traversal": "reference order (FP64, bit-identical to the reference)",
+            "seeding": "plain (triangle 0 of each model, as after EndModel)",
+            "contacts_per_query": CONTACT_SLOTS, "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    args = parse()
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo" if args.impl == "reference" else "nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    from c2a_gb300 import api, build
+
+    torch.cuda.set_device(local)
+    if rank == 0:
+        build.build()
+    if dist:
+        dist.barrier()
+    wl = workloads.config2(n=args.queries, seed=2 + rank, device=f"cuda:{local}")
+    ctx = api.Context(local)
+    mid = ctx.model(wl.meshes[0])
+    qint = wl.qint.copy()
+    qint[:, :2] = mid
+    qs = api.make_queries(qint, wl.poses)
+    n = wl.n
+    d_q = torch.from_numpy(qs.view(np.uint8).copy()).cuda()
+    d_r = torch.zeros(n * api.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_c = torch.zeros(n * CONTACT_SLOTS * api.CONTACT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def step():
+        ctx.solve_device(d_q.data_ptr(), n, wl.params, d_r.data_ptr(), d_c.data_ptr(), CONTACT_SLOTS,
+                         stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    launches0 = ctx.launches()
+    clocks = Clocks(local)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()  # evict queries, models and results from L2 before each timed step
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        dist.barrier()
+    launches = ctx.launches() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    res = d_r.cpu().numpy().view(api.RESULT_DTYPE)
+    if (res["status"] & ~(api.QUERY_ITER_CAP | api.QUERY_CONTACT_OVERFLOW)).any():
+        raise RuntimeError("a query reported a failure status")
+    value = n * world * args.steps / (total_ms / 1000.0)
+
+    # roofline of the CA kernel: algorithmic node/triangle bytes per launch / launch time
+    bv = int(res["num_bv_tests"].sum())
+    tri = int(res["num_tri_tests"].sum())
+    alg_bytes = bv * NODE_BYTES + tri * TRI_BYTES
+    launch_s = (total_ms / args.steps) / 1000.0
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = alg_bytes / launch_s / 1e9
+    prof = profile_traffic()
+    traffic = None
+    if prof and prof.get("dram_bytes_per_query"):
+        traffic = float(prof["dram_bytes_per_query"]) * n
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": peak_src, "kernel": "c2a_solve_kernel",
+                "algorithmic_bytes_per_launch": alg_bytes, "num_bv_tests": bv, "num_tri_tests": tri,
+                "note": "the kernel is FP64-instruction bound (GB300 FP64 ~1/64 of FP32); node bytes are "
+                        "the reference's algorithmic reads, mostly served by L2"}
+
+    e2e = None
+    if not args.no_e2e:
+        rr, cc = ctx.solve(qint, wl.poses, wl.params, contacts_per_query=CONTACT_SLOTS)  # warm the host path
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        totals = []
+        for _ in range(args.steps):
+            rr, cc = ctx.solve(qint, wl.poses, wl.params, contacts_per_query=CONTACT_SLOTS)
+            totals.append(cc.total())
+        e2e_s = time.perf_counter() - t0
+        te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e_s = float(te.item())
+        e2e = {"value": n * world * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": n * api.QUERY_DTYPE.itemsize,
+               "d2h_bytes_per_step": int(n * api.RESULT_DTYPE.itemsize + np.mean(totals) * api.CONTACT_DTYPE.itemsize
+                                         + 4),
+               "api": "c2a_solve_batch (host buffers)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = args.cpu_sample or auto_sample(wl, threads)
+        rate, dt, pres = cpu_baseline(wl, sample, threads)
+        same = bool((pres["toc"].tobytes() == res["toc"][:len(pres)].tobytes()) and
+                    np.array_equal(pres["numCA"], res["numCA"][:len(pres)]))
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"first {len(pres)} of the {n} queries ({dt:.1f} s wall on {threads} threads)",
+               "bit_identical_to_gpu": same}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
+                "config": config_dict(wl, args), "clocks": clk, "gpu_launches": launches, "e2e": e2e,
+                "roofline": roofline, "cpu_baseline": cpu,
+                "collision_fraction": float(1 - res["collisionfree"].mean()),
+                "mean_numCA": float(res["numCA"].mean()), "step_ms": step_ms}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,656 @@
+/*
+ * c2a_abi.cu -- the C ABI of include/c2a_gb300.h: contexts, model upload and
+ * the CA kernels' launches.  Everything the reference computes per query runs
+ * on the GPU; the host only builds the BVH (as the reference's EndModel
+ * does), moves buffers and launches.
+ */
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/c2a_gb300.h"
+#include "device/ca_kernel.cuh"
+#include "host/bvh_build.h"
+
+using namespace c2a;
+
+namespace {
+
+constexpr int kThreads = 128;
+
+struct ModelSlot {
+    BuiltModel host;
+    NodeRec *d_nodes = nullptr;
+    TriRec *d_tris = nullptr;
+    bool live = false;
+};
+
+} // namespace
+
+struct c2a_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<ModelSlot> models;
+    DevModel *d_models = nullptr;
+    int d_models_cap = 0;
+    bool models_dirty = true;
+    unsigned int *d_counter = nullptr; /* work counter of the persistent kernels */
+    int64_t launches = 0;
+    /* device staging for the host-buffer entry points */
+    void *d_buf = nullptr;
+    size_t d_buf_size = 0;
+    int32_t last_contacts = 0; /* contacts copied back by the last c2a_solve_batch */
+    std::mutex mu;
+};
+
+namespace {
+
+c2a_status cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return C2A_OK;
+    if (e == cudaErrorMemoryAllocation) return C2A_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return C2A_ERR_NO_DEVICE;
+    return C2A_ERR_CUDA;
+}
+
+#define C2A_CUDA(call)                                                                                             \
+    do {                                                                                                           \
+        cudaError_t e_ = (call);                                                                                   \
+        if (e_ != cudaSuccess) {                                                                                   \
+            fprintf(stderr, "c2a_gb300: %s failed: %s\n", #call, cudaGetErrorString(e_));                          \
+            return cuda_status(e_);                                                                                \
+        }                                                                                                          \
+    } while (0)
+
+/* uploads the model table when models were added or freed */
+c2a_status sync_models(c2a_context *ctx)
+{
+    if (!ctx->models_dirty) return C2A_OK;
+    std::vector<DevModel> table(ctx->models.size());
+    for (size_t i = 0; i < ctx->models.size(); i++) {
+        const ModelSlot &s = ctx->models[i];
+        table[i].nodes = s.d_nodes;
+        table[i].tris = s.d_tris;
+        table[i].num_tris = s.live ? (int32_t)s.host.tris.size() : 0;
+        table[i].num_nodes = s.live ? (int32_t)s.host.nodes.size() : 0;
+        table[i].depth = s.host.depth;
+        table[i].live = s.live ? 1 : 0;
+    }
+    if ((int)table.size() > ctx->d_models_cap) {
+        if (ctx->d_models) cudaFree(ctx->d_models);
+        ctx->d_models = nullptr;
+        int cap = (int)table.size() * 2 + 4;
+        C2A_CUDA(cudaMalloc(&ctx->d_models, sizeof(DevModel) * cap));
+        ctx->d_models_cap = cap;
+    }
+    if (!table.empty())
+        C2A_CUDA(cudaMemcpyAsync(ctx->d_models, table.data(), sizeof(DevModel) * table.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->models_dirty = false;
+    return C2A_OK;
+}
+
+c2a_status ensure_buf(c2a_context *ctx, size_t bytes)
+{
+    if (bytes <= ctx->d_buf_size) return C2A_OK;
+    if (ctx->d_buf) cudaFree(ctx->d_buf);
+    ctx->d_buf = nullptr;
+    ctx->d_buf_size = 0;
+    size_t sz = bytes + bytes / 4 + 4096;
+    C2A_CUDA(cudaMalloc(&ctx->d_buf, sz));
+    ctx->d_buf_size = sz;
+    return C2A_OK;
+}
+
+bool params_ok(const c2a_params *p)
+{
+    return p && p->max_iters >= 0 && p->contacts_per_query >= 0;
+}
+
+/* queries must not pair models deeper than the traversal stack */
+c2a_status check_depths(c2a_context *ctx)
+{
+    int deepest = 0;
+    for (const ModelSlot &s : ctx->models)
+        if (s.live && s.host.depth > deepest) deepest = s.host.depth;
+    if (2 * deepest + 2 > C2A_STACK_DEPTH) return C2A_ERR_TREE_TOO_DEEP;
+    return C2A_OK;
+}
+
+int grid_for(c2a_context *ctx, int n)
+{
+    int blocks = ctx->sm_count * 8;
+    int need = (n + kThreads - 1) / kThreads;
+    return need < blocks ? (need > 0 ? need : 1) : blocks;
+}
+
+} // namespace
+
+/* ------------------------------------------------------------- kernels */
+
+__global__ void __launch_bounds__(kThreads) c2a_solve_kernel(const c2a_query *__restrict__ queries, int n,
+                                                             const DevModel *__restrict__ models, int num_models,
+                                                             c2a_params prm, c2a_result *__restrict__ results,
+                                                             c2a_contact *__restrict__ contacts,
+                                                             unsigned int *__restrict__ counter)
+{
+    StackEntry stack[C2A_STACK_DEPTH];
+    for (;;) {
+        const unsigned int q = atomicAdd(counter, 1u);
+        if (q >= (unsigned int)n) break;
+        c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
+        solve_query(queries[q], models, num_models, prm, results[q], cq, stack, (int)q);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) c2a_step_kernel(const c2a_query *__restrict__ queries, int n,
+                                                            const double *__restrict__ lambda,
+                                                            const int32_t *__restrict__ num_ca,
+                                                            const double *__restrict__ prev_mint,
+                                                            const DevModel *__restrict__ models, int num_models,
+                                                            c2a_params prm, c2a_result *__restrict__ results)
+{
+    StackEntry stack[C2A_STACK_DEPTH];
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= n) return;
+    const c2a_query &in = queries[qi];
+    c2a_result &out = results[qi];
+    out.status = 0;
+    if (in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 || in.model_b >= num_models ||
+        !models[in.model_a].live || !models[in.model_b].live) {
+        out.status = C2A_QUERY_BAD_INPUT;
+        return;
+    }
+    Query q;
+    q.A = models + in.model_a;
+    q.B = models + in.model_b;
+    if (in.seed_a < 0 || in.seed_a >= q.A->num_tris || in.seed_b < 0 || in.seed_b >= q.B->num_tris) {
+        out.status = C2A_QUERY_BAD_INPUT;
+        return;
+    }
+    q.status = 0;
+    const double *P = in.pose;
+    motion_setup(q.m1, P, P + 9, P + 12, P + 21);
+    motion_setup(q.m2, P + 24, P + 33, P + 36, P + 45);
+    q.toc_delta = prm.toc_delta;
+    const bool translation = (q.m1.angVel < 1e-8 && q.m2.angVel < 1e-8);
+    const double lam = lambda[qi];
+    M3 R1, R2;
+    V3 T1, T2;
+    if (lam == 0.0) {
+        R1 = pose_R(P);
+        T1 = pose_T(P);
+        R2 = pose_R(P + 24);
+        T2 = pose_T(P + 24);
+    } else {
+        double orn[4];
+        motion_integrate(q.m1, lam, R1.m, &T1.x, orn);
+        motion_integrate(q.m2, lam, R2.m, &T2.x, orn);
+    }
+    q.r1 = R1;
+    q.t1 = T1;
+    q.seed_a = in.seed_a;
+    q.seed_b = in.seed_b;
+    q.nbv = q.ntri = 0;
+    q.numCA = num_ca[qi];
+    q.mint = prev_mint[qi];
+    q.upbound = 1.0 - lam;
+    q.distance = 0;
+    toc_step(q, R1, T1, R2, T2, translation, stack);
+    out.collisionfree = 0;
+    out.numCA = q.numCA;
+    out.translation = translation ? 1 : 0;
+    out.num_contact = 0;
+    out.toc = lam;
+    out.distance = q.distance;
+    out.mint = q.mint;
+    out.num_bv_tests = q.nbv;
+    out.num_tri_tests = q.ntri;
+    out.seed_a = q.seed_a;
+    out.seed_b = q.seed_b;
+    out.status = q.status;
+}
+
+__global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *__restrict__ queries, int n,
+                                                               const double *__restrict__ threshold,
+                                                               const DevModel *__restrict__ models, int num_models,
+                                                               int slots, c2a_result *__restrict__ results,
+                                                               c2a_contact *__restrict__ contacts)
+{
+    StackEntry stack[C2A_STACK_DEPTH];
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= n) return;
+    const c2a_query &in = queries[qi];
+    c2a_result &out = results[qi];
+    out.status = 0;
+    out.num_contact = 0;
+    if (in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 || in.model_b >= num_models ||
+        !models[in.model_a].live || !models[in.model_b].live) {
+        out.status = C2A_QUERY_BAD_INPUT;
+        return;
+    }
+    Query q;
+    q.A = models + in.model_a;
+    q.B = models + in.model_b;
+    q.status = 0;
+    const double *P = in.pose;
+    M3 R;
+    V3 T;
+    relative_transforms(q, pose_R(P), pose_T(P), pose_R(P + 24), pose_T(P + 24), R, T);
+    const int cnt = contact_dfs(q, R, T, threshold[qi], stack,
+                                contacts ? contacts + (size_t)qi * (size_t)slots : nullptr, slots, qi);
+    out.num_contact = cnt;
+    out.contact_offset = qi * slots;
+    out.status = q.status | (cnt > slots ? C2A_QUERY_CONTACT_OVERFLOW : 0);
+}
+
+/* dense contact output: exclusive scan of min(num_contact, slots), then a
+ * gather of the used slots (one block per 1024 queries, block-local scan
+ * followed by a scan of the block totals) */
+constexpr int kScanBlock = 1024;
+
+__global__ void __launch_bounds__(kScanBlock) c2a_scan_blocks(c2a_result *__restrict__ results, int n, int slots,
+                                                               int32_t *__restrict__ block_sums)
+{
+    __shared__ int32_t s[kScanBlock];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    int32_t v = 0;
+    if (i < n) {
+        const int32_t c = results[i].num_contact;
+        v = c < slots ? c : slots;
+    }
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        int32_t t = threadIdx.x >= off ? s[threadIdx.x - off] : 0;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) results[i].contact_offset = s[threadIdx.x] - v; /* block-local exclusive */
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void c2a_scan_totals(int32_t *__restrict__ block_sums, int nblocks, int32_t *__restrict__ total)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int32_t run = 0;
+    for (int b = 0; b < nblocks; b++) {
+        const int32_t t = block_sums[b];
+        block_sums[b] = run;
+        run += t;
+    }
+    *total = run;
+}
+
+__global__ void c2a_gather_contacts(c2a_result *__restrict__ results, int n, int slots,
+                                    const int32_t *__restrict__ block_sums, const c2a_contact *__restrict__ src,
+                                    c2a_contact *__restrict__ dst)
+{
+    const int q = blockIdx.x;
+    if (q >= n) return;
+    const int off = results[q].contact_offset + block_sums[q / kScanBlock];
+    const int c = results[q].num_contact < slots ? results[q].num_contact : slots;
+    for (int k = threadIdx.x; k < c; k += blockDim.x) dst[off + k] = src[(size_t)q * slots + k];
+    __syncthreads();
+    if (threadIdx.x == 0) results[q].contact_offset = off;
+}
+
+/* --------------------------------------------------------------- ABI */
+
+extern "C" {
+
+const char *c2a_status_str(c2a_status s)
+{
+    switch (s) {
+    case C2A_OK: return "ok";
+    case C2A_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case C2A_ERR_NO_DEVICE: return "no CUDA device";
+    case C2A_ERR_CUDA: return "CUDA error";
+    case C2A_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case C2A_ERR_EMPTY_MODEL: return "model has no triangles";
+    case C2A_ERR_BAD_MODEL: return "unknown model id";
+    case C2A_ERR_TREE_TOO_DEEP: return "hierarchy deeper than the traversal stack";
+    case C2A_ERR_QUERY_FAILED: return "a query reported a non-zero status";
+    default: return "unknown status";
+    }
+}
+
+c2a_status c2a_create(int device, c2a_context **out)
+{
+    if (!out) return C2A_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (device == -1) { /* host-only: builds and downloads models, runs no query */
+        c2a_context *ctx = new (std::nothrow) c2a_context();
+        if (!ctx) return C2A_ERR_OUT_OF_MEMORY;
+        ctx->device = -1;
+        *out = ctx;
+        return C2A_OK;
+    }
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return C2A_ERR_NO_DEVICE;
+    if (device < 0 || device >= count) return C2A_ERR_INVALID_ARGUMENT;
+    C2A_CUDA(cudaSetDevice(device));
+    c2a_context *ctx = new (std::nothrow) c2a_context();
+    if (!ctx) return C2A_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->d_counter, sizeof(unsigned int) * 4) != cudaSuccess) {
+        c2a_destroy(ctx);
+        return C2A_ERR_CUDA;
+    }
+    *out = ctx;
+    return C2A_OK;
+}
+
+c2a_status c2a_destroy(c2a_context *ctx)
+{
+    if (!ctx) return C2A_OK;
+    if (ctx->device < 0) {
+        delete ctx;
+        return C2A_OK;
+    }
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (ModelSlot &s : ctx->models) {
+        if (s.d_nodes) cudaFree(s.d_nodes);
+        if (s.d_tris) cudaFree(s.d_tris);
+    }
+    if (ctx->d_models) cudaFree(ctx->d_models);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
+    if (ctx->d_buf) cudaFree(ctx->d_buf);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return C2A_OK;
+}
+
+c2a_status c2a_launch_count(c2a_context *ctx, int64_t *count)
+{
+    if (!ctx || !count) return C2A_ERR_INVALID_ARGUMENT;
+    *count = ctx->launches;
+    return C2A_OK;
+}
+
+c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
+                           const int32_t *vidx, int32_t *model_id)
+{
+    if (!ctx || !model_id) return C2A_ERR_INVALID_ARGUMENT;
+    ModelSlot slot;
+    int rc = build_rss_model(num_tris, tri_verts, ids, vidx, slot.host);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (ctx->device < 0) {
+        slot.live = true;
+        ctx->models.push_back(std::move(slot));
+        *model_id = (int32_t)ctx->models.size() - 1;
+        return C2A_OK;
+    }
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    C2A_CUDA(cudaMalloc(&slot.d_nodes, sizeof(NodeRec) * slot.host.nodes.size()));
+    C2A_CUDA(cudaMalloc(&slot.d_tris, sizeof(TriRec) * slot.host.tris.size()));
+    C2A_CUDA(cudaMemcpyAsync(slot.d_nodes, slot.host.nodes.data(), sizeof(NodeRec) * slot.host.nodes.size(),
+                             cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaMemcpyAsync(slot.d_tris, slot.host.tris.data(), sizeof(TriRec) * slot.host.tris.size(),
+                             cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    slot.live = true;
+    ctx->models.push_back(std::move(slot));
+    ctx->models_dirty = true;
+    *model_id = (int32_t)ctx->models.size() - 1;
+    return C2A_OK;
+}
+
+c2a_status c2a_model_info(c2a_context *ctx, int32_t id, int32_t *num_tris, int32_t *num_nodes, int32_t *depth)
+{
+    if (!ctx) return C2A_ERR_INVALID_ARGUMENT;
+    if (id < 0 || id >= (int32_t)ctx->models.size() || !ctx->models[id].live) return C2A_ERR_BAD_MODEL;
+    const BuiltModel &m = ctx->models[id].host;
+    if (num_tris) *num_tris = (int32_t)m.tris.size();
+    if (num_nodes) *num_nodes = (int32_t)m.nodes.size();
+    if (depth) *depth = m.depth;
+    return C2A_OK;
+}
+
+c2a_status c2a_model_download(c2a_context *ctx, int32_t id, double *node_f, int32_t *first_child, double *tri_verts,
+                              int32_t *tri_ids, int32_t *tri_vidx)
+{
+    if (!ctx) return C2A_ERR_INVALID_ARGUMENT;
+    if (id < 0 || id >= (int32_t)ctx->models.size() || !ctx->models[id].live) return C2A_ERR_BAD_MODEL;
+    const BuiltModel &m = ctx->models[id].host;
+    for (size_t i = 0; i < m.nodes.size(); i++) {
+        const NodeRec &n = m.nodes[i];
+        if (node_f) {
+            double *o = node_f + 25 * i;
+            std::memcpy(o, n.R, sizeof(n.R));
+            std::memcpy(o + 9, n.Tr, sizeof(n.Tr));
+            o[12] = n.l[0];
+            o[13] = n.l[1];
+            o[14] = n.r;
+            o[15] = n.angR;
+            std::memcpy(o + 16, n.Rloc, sizeof(n.Rloc));
+        }
+        if (first_child) first_child[i] = n.first_child;
+    }
+    for (size_t i = 0; i < m.tris.size(); i++) {
+        const TriRec &t = m.tris[i];
+        if (tri_verts) std::memcpy(tri_verts + 9 * i, t.v, sizeof(t.v));
+        if (tri_ids) tri_ids[i] = t.id;
+        if (tri_vidx)
+            for (int k = 0; k < 3; k++) tri_vidx[3 * i + k] = t.idx[k];
+    }
+    return C2A_OK;
+}
+
+c2a_status c2a_model_free(c2a_context *ctx, int32_t id)
+{
+    if (!ctx) return C2A_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (id < 0 || id >= (int32_t)ctx->models.size() || !ctx->models[id].live) return C2A_ERR_BAD_MODEL;
+    ModelSlot &s = ctx->models[id];
+    if (ctx->device >= 0) {
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(s.d_nodes);
+        cudaFree(s.d_tris);
+    }
+    s.d_nodes = nullptr;
+    s.d_tris = nullptr;
+    s.live = false;
+    s.host = BuiltModel();
+    ctx->models_dirty = true;
+    return C2A_OK;
+}
+
+c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
+                                  c2a_result *d_results, c2a_contact *d_contacts, void *stream)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    c2a_status st = check_depths(ctx);
+    if (st) return st;
+    st = sync_models(ctx);
+    if (st) return st;
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
+    c2a_params prm = *params;
+    if (!d_contacts) prm.contacts_per_query = 0;
+    c2a_solve_kernel<<<grid_for(ctx, n), kThreads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(),
+                                                            prm, d_results, d_contacts, ctx->d_counter);
+    ctx->launches++;
+    C2A_CUDA(cudaGetLastError());
+    return C2A_OK;
+}
+
+c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const c2a_params *params,
+                           c2a_result *results, c2a_contact *contacts)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!queries || !results))) return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    const size_t nq = (size_t)n;
+    const size_t cpq = contacts ? (size_t)params->contacts_per_query : 0;
+    const size_t nblocks = (nq + kScanBlock - 1) / kScanBlock;
+    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
+    const size_t qbytes = up(sizeof(c2a_query) * nq), rbytes = up(sizeof(c2a_result) * nq);
+    const size_t cbytes = up(sizeof(c2a_contact) * nq * cpq), sbytes = up(sizeof(int32_t) * (nblocks + 1));
+    c2a_status st = ensure_buf(ctx, qbytes + rbytes + 2 * cbytes + sbytes);
+    if (st) return st;
+    char *base = (char *)ctx->d_buf;
+    c2a_query *dq = (c2a_query *)base;
+    c2a_result *dr = (c2a_result *)(base + qbytes);
+    c2a_contact *dc = cpq ? (c2a_contact *)(base + qbytes + rbytes) : nullptr;
+    c2a_contact *dense = cpq ? (c2a_contact *)(base + qbytes + rbytes + cbytes) : nullptr;
+    int32_t *sums = (int32_t *)(base + qbytes + rbytes + 2 * cbytes);
+    C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    c2a_params prm = *params;
+    if (!cpq) prm.contacts_per_query = 0;
+    st = c2a_solve_batch_device(ctx, dq, n, &prm, dr, dc, ctx->stream);
+    if (st) return st;
+    int32_t total = 0;
+    if (cpq) {
+        c2a_scan_blocks<<<(unsigned)nblocks, kScanBlock, 0, ctx->stream>>>(dr, n, (int)cpq, sums);
+        c2a_scan_totals<<<1, 1, 0, ctx->stream>>>(sums, (int)nblocks, sums + nblocks);
+        c2a_gather_contacts<<<(unsigned)nq, 32, 0, ctx->stream>>>(dr, n, (int)cpq, sums, dc, dense);
+        ctx->launches += 3;
+        C2A_CUDA(cudaGetLastError());
+        C2A_CUDA(cudaMemcpyAsync(&total, sums + nblocks, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (cpq && total > 0) {
+        C2A_CUDA(cudaMemcpyAsync(contacts, dense, sizeof(c2a_contact) * (size_t)total, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+        C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->last_contacts = total;
+    for (int32_t i = 0; i < n; i++)
+        if (results[i].status & ~(C2A_QUERY_ITER_CAP | C2A_QUERY_CONTACT_OVERFLOW)) return C2A_ERR_QUERY_FAILED;
+    return C2A_OK;
+}
+
+c2a_status c2a_toc_step_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *lambda,
+                              const int32_t *num_ca, const double *prev_mint, const c2a_params *params,
+                              c2a_result *results)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!queries || !lambda || !num_ca || !prev_mint || !results)))
+        return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    c2a_status st = check_depths(ctx);
+    if (st) return st;
+    st = sync_models(ctx);
+    if (st) return st;
+    const size_t nq = (size_t)n;
+    const size_t a = ((sizeof(c2a_query) * nq + 255) / 256) * 256, b = ((sizeof(double) * nq + 255) / 256) * 256;
+    const size_t c = ((sizeof(int32_t) * nq + 255) / 256) * 256, r = sizeof(c2a_result) * nq;
+    st = ensure_buf(ctx, a + 2 * b + c + r);
+    if (st) return st;
+    char *base = (char *)ctx->d_buf;
+    c2a_query *dq = (c2a_query *)base;
+    double *dl = (double *)(base + a);
+    double *dm = (double *)(base + a + b);
+    int32_t *dn = (int32_t *)(base + a + 2 * b);
+    c2a_result *dr = (c2a_result *)(base + a + 2 * b + c);
+    C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaMemcpyAsync(dl, lambda, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaMemcpyAsync(dm, prev_mint, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaMemcpyAsync(dn, num_ca, sizeof(int32_t) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    c2a_step_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
+        dq, n, dl, dn, dm, ctx->d_models, (int)ctx->models.size(), *params, dr);
+    ctx->launches++;
+    C2A_CUDA(cudaGetLastError());
+    C2A_CUDA(cudaMemcpyAsync(results, dr, r, cudaMemcpyDeviceToHost, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int32_t i = 0; i < n; i++)
+        if (results[i].status) return C2A_ERR_QUERY_FAILED;
+    return C2A_OK;
+}
+
+c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *threshold,
+                                  int32_t contacts_per_query, c2a_result *results, c2a_contact *contacts)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || contacts_per_query < 0 || (n > 0 && (!queries || !threshold || !results)))
+        return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    c2a_status st = check_depths(ctx);
+    if (st) return st;
+    st = sync_models(ctx);
+    if (st) return st;
+    const size_t nq = (size_t)n, cpq = contacts ? (size_t)contacts_per_query : 0;
+    const size_t a = ((sizeof(c2a_query) * nq + 255) / 256) * 256, b = ((sizeof(double) * nq + 255) / 256) * 256;
+    const size_t r = ((sizeof(c2a_result) * nq + 255) / 256) * 256, cb = sizeof(c2a_contact) * nq * cpq;
+    st = ensure_buf(ctx, a + b + r + cb);
+    if (st) return st;
+    char *base = (char *)ctx->d_buf;
+    c2a_query *dq = (c2a_query *)base;
+    double *dt = (double *)(base + a);
+    c2a_result *dr = (c2a_result *)(base + a + b);
+    c2a_contact *dc = cpq ? (c2a_contact *)(base + a + b + r) : nullptr;
+    C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    C2A_CUDA(cudaMemcpyAsync(dt, threshold, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    c2a_contact_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
+        dq, n, dt, ctx->d_models, (int)ctx->models.size(), (int)cpq, dr, dc);
+    ctx->launches++;
+    C2A_CUDA(cudaGetLastError());
+    C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));
+    if (cpq) C2A_CUDA(cudaMemcpyAsync(contacts, dc, cb, cudaMemcpyDeviceToHost, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int32_t i = 0; i < n; i++)
+        if (results[i].status & ~C2A_QUERY_CONTACT_OVERFLOW) return C2A_ERR_QUERY_FAILED;
+    return C2A_OK;
+}
+
+c2a_status c2a_motion_setup(const double *R0, const double *T0, const double *R1, const double *T1, double *out)
+{
+    if (!R0 || !T0 || !R1 || !T1 || !out) return C2A_ERR_INVALID_ARGUMENT;
+    Motion m;
+    motion_setup(m, R0, T0, R1, T1);
+    for (int i = 0; i < 3; i++) {
+        out[i] = m.axis[i];
+        out[4 + i] = m.cv[i];
+    }
+    out[3] = m.angVel;
+    for (int i = 0; i < 4; i++) out[7 + i] = m.q0[i];
+    return C2A_OK;
+}
+
+c2a_status c2a_motion_integrate(const double *R0, const double *T0, const double *R1, const double *T1, double t,
+                                double *R, double *T, double *qua)
+{
+    if (!R0 || !T0 || !R1 || !T1) return C2A_ERR_INVALID_ARGUMENT;
+    Motion m;
+    motion_setup(m, R0, T0, R1, T1);
+    double Rr[9], Tt[3], orn[4];
+    motion_integrate(m, t, Rr, Tt, orn);
+    if (R) std::memcpy(R, Rr, sizeof(Rr));
+    if (T) std::memcpy(T, Tt, sizeof(Tt));
+    if (qua) {
+        qua[0] = orn[3];
+        qua[1] = orn[0];
+        qua[2] = orn[1];
+        qua[3] = orn[2];
+        qua[4] = Tt[0];
+        qua[5] = Tt[1];
+        qua[6] = Tt[2];
+    }
+    return C2A_OK;
+}
+
+} // extern "C"

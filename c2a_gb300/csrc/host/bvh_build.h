@@ -1,0 +1,58 @@
+/*
+ * bvh_build.h -- host build of C2A's RSS bounding-volume hierarchy and the
+ * node/triangle records the kernels read from HBM.
+ */
+#ifndef C2A_BVH_BUILD_H
+#define C2A_BVH_BUILD_H
+
+#include <cstdint>
+#include <vector>
+
+namespace c2a {
+
+/*
+ * One BVH node as the CUDA kernels load it: 256 bytes, 16-byte aligned so a
+ * node is thirteen 128-bit loads, two 128-byte lines.  Fields are those the CA
+ * path reads from C2A_BV (C2A/C2A_BV.h:33-77, PQP BV): parent-relative R and
+ * Tr, rectangle lengths l, radius r, angularRadius, build-time R_loc, plus
+ * the split measure GetSize() = |l| + 2r precomputed with the same
+ * arithmetic.
+ */
+struct alignas(16) NodeRec {
+    double R[9];
+    double Tr[3];
+    double l[2];
+    double r;
+    double angR;
+    double Rloc[9];
+    double size;
+    int32_t first_child; /* >= 0: first of two children; < 0: -(triangle) - 1 */
+    int32_t depth;       /* depth below the root */
+    double pad[5];
+};
+static_assert(sizeof(NodeRec) == 256, "node record must stay 256 bytes");
+
+/* One triangle, post-build order: vertices, caller id, caller vertex indices. */
+struct alignas(16) TriRec {
+    double v[9];
+    int32_t id;
+    int32_t idx[3];
+    double pad;
+};
+static_assert(sizeof(TriRec) == 96, "triangle record must stay 96 bytes");
+
+struct BuiltModel {
+    std::vector<NodeRec> nodes;
+    std::vector<TriRec> tris;
+    int32_t depth = 0; /* maximum node depth (root = 0) */
+};
+
+/* C2A_Model::EndModel + C2A_BuildModel: returns 0 or a C2A_ERR_* code. */
+int build_rss_model(int32_t num_tris, const double *tri_verts, const int32_t *ids, const int32_t *vidx,
+                    BuiltModel &out);
+
+/* Symmetric 3x3 eigen-decomposition (columns of v are eigenvectors). */
+void jacobi_eigen3(double v[3][3], double d[3], const double a[3][3]);
+
+} // namespace c2a
+#endif

@@ -1,0 +1,179 @@
+/*
+ * c2a_gb300.h -- C ABI of the GB300-native C2A conservative-advancement (CA)
+ * library (libc2a_gb300.so).  Plain pointers and sizes only; every call
+ * returns a c2a_status.  This is the boundary a host program, a ctypes/cgo
+ * binding, or the C++ drop-in API (c2a_gb300_cpp.h) binds to.
+ *
+ * Reference interfaces replaced (paths within EwhaGlab/C2A):
+ *   c2a_model_build          C2A_Model::BeginModel/AddTri/EndModel
+ *                            (C2A/src/C2A_PQP.cpp:82-417) with the RSS
+ *                            hierarchy build of C2A_BuildModel
+ *                            (C2A/src/C2A_Build.cpp:546-574)
+ *   c2a_solve_batch          C2A_Solve (C2A/C2A.h:23-35, C2A/src/C2A.cpp:2315)
+ *                            over many independent queries; each query is
+ *                            C2A_QueryTimeOfContact (C2A/C2A.h:274-281)
+ *                            followed, when not collision free, by
+ *                            C2A_QueryContact (C2A/C2A.h:284-290)
+ *   c2a_toc_step_batch       C2A_TimeOfContactStep (C2A/src/C2A.cpp:1778-1789)
+ *   c2a_contact_only_batch   C2A_QueryContactOnly (C2A/C2A.h:292-299)
+ *   c2a_motion_setup         CInterpMotion_Linear ctor/velocity
+ *                            (C2A/src/InterpMotion.cpp:494-502, 228-270)
+ *   c2a_motion_integrate     CInterpMotion_Linear::integrate
+ *                            (C2A/src/InterpMotion.cpp:516-568)
+ *
+ * Semantics follow the reference exactly (FP64, same evaluation order; the
+ * reference's C2A_Solve hard-codes tolerance_d = m_toc_delta = 1e-4 and
+ * ignores th_ca, here they are parameters).  Results are bit-identical to the
+ * reference on the same inputs.
+ */
+#ifndef C2A_GB300_H
+#define C2A_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t c2a_status;
+enum {
+    C2A_OK = 0,
+    C2A_ERR_INVALID_ARGUMENT = 1,
+    C2A_ERR_NO_DEVICE = 2,
+    C2A_ERR_CUDA = 3,
+    C2A_ERR_OUT_OF_MEMORY = 4,
+    C2A_ERR_EMPTY_MODEL = 5,      /* PQP_ERR_BUILD_EMPTY_MODEL (C2A_PQP.cpp:352-357) */
+    C2A_ERR_BAD_MODEL = 6,        /* unknown or freed model id */
+    C2A_ERR_TREE_TOO_DEEP = 7,    /* BVTT deeper than the traversal stack */
+    C2A_ERR_QUERY_FAILED = 8      /* at least one query has a non-zero status */
+};
+
+/* per-query status word (c2a_result.status), bit flags */
+enum {
+    C2A_QUERY_OK = 0,
+    C2A_QUERY_BAD_INPUT = 1,        /* model id or seed triangle out of range */
+    C2A_QUERY_STACK_OVERFLOW = 2,   /* traversal stack exhausted (never with checked models) */
+    C2A_QUERY_CONTACT_OVERFLOW = 4, /* more contacts than contacts_per_query (num_contact is still exact) */
+    C2A_QUERY_ITER_CAP = 8          /* hit max_iters; reported as contact at the last lambda, like the reference */
+};
+
+typedef struct c2a_context c2a_context;
+
+/* Query: two models, the seed pair (C2A's dres.last_triA/B, post-build
+ * triangle indices) and the four poses of C2A_Solve, each row-major R(9) then
+ * T(3): A at t=0, A at t=1, B at t=0, B at t=1 (48 doubles). */
+typedef struct c2a_query {
+    int32_t model_a, model_b;
+    int32_t seed_a, seed_b;
+    double pose[48];
+} c2a_query;
+
+typedef struct c2a_params {
+    double tol_d;        /* tolerance_d (C2A_Solve: 1e-4, C2A.cpp:2384) */
+    double tol_t;        /* tolerance_t (C2A_Solve: 1e-4, C2A.cpp:2385) */
+    double toc_delta;    /* CInterpMotion::m_toc_delta (C2A_Solve: 1e-4) */
+    double contact_abs;  /* contact threshold = 2 d + contact_abs (C2A.cpp:2433: 0.001) */
+    int32_t with_contacts;      /* enumerate contacts at the TOC */
+    int32_t max_iters;          /* CA iteration cap (reference: 150) */
+    int32_t qsize;              /* front capacity hint; never changes a result */
+    int32_t contacts_per_query; /* contact slots per query in the output buffer */
+} c2a_params;
+
+typedef struct c2a_result {
+    int32_t collisionfree;
+    int32_t numCA;
+    int32_t translation;   /* both angular speeds < 1e-8: translation-only CA */
+    int32_t num_contact;   /* all contacts found (may exceed contacts_per_query) */
+    double toc;
+    double distance;       /* res->distance after the last CA step */
+    double mint;           /* res->mint after the last CA step */
+    int64_t num_bv_tests;  /* reference counters (C2A.cpp:1180, 1279) */
+    int64_t num_tri_tests;
+    double R_toc[2][9];    /* poses at the TOC (when not collision free) */
+    double T_toc[2][3];
+    int32_t seed_a, seed_b; /* seed pair after the query */
+    int32_t status;        /* C2A_QUERY_* flags */
+    int32_t contact_offset; /* first of this query's contacts in the contact buffer */
+} c2a_result;
+
+/* One contact pair (ContactF, C2A/C2A.h:116-158), in the order the reference
+ * visits them (its list is built with push_front, so reversed). */
+typedef struct c2a_contact {
+    int32_t type_a, type_b;         /* 1 vertex, 2 edge, 3 face */
+    int32_t fid_a[3], fid_b[3];     /* caller vertex indices of the features, -1 unused */
+    int32_t tri_a, tri_b;           /* post-build triangle indices */
+    int32_t query, pad;             /* index of the query in its batch */
+    double pa[3], pb[3];            /* closest points, each in its own model frame */
+    double distance;
+} c2a_contact;
+
+/* ---- context --------------------------------------------------------- */
+/* device >= 0: a CUDA device; device == -1: a host-only context that builds
+ * and downloads models but runs no query (C2A_ERR_NO_DEVICE). */
+c2a_status c2a_create(int device, c2a_context **ctx);
+c2a_status c2a_destroy(c2a_context *ctx);
+const char *c2a_status_str(c2a_status s);
+/* number of kernel launches issued by this context so far */
+c2a_status c2a_launch_count(c2a_context *ctx, int64_t *count);
+
+/* ---- models ---------------------------------------------------------- */
+/* Builds the RSS hierarchy of a triangle soup on the host (bit-identical to
+ * the reference's EndModel) and uploads it.  tri_verts: num_tris x 9 doubles
+ * (p1, p2, p3); ids and vidx (num_tris x 3) may be NULL. */
+c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
+                           const int32_t *vidx, int32_t *model_id);
+c2a_status c2a_model_info(c2a_context *ctx, int32_t model_id, int32_t *num_tris, int32_t *num_nodes,
+                          int32_t *depth);
+/* Host copy of the built hierarchy: node_f num_nodes x 25 doubles (R 9, Tr 3,
+ * l 2, r, angularRadius, R_loc 9), first_child, triangles in post-build
+ * order (9 doubles, id, 3 vertex indices). */
+c2a_status c2a_model_download(c2a_context *ctx, int32_t model_id, double *node_f, int32_t *first_child,
+                              double *tri_verts, int32_t *tri_ids, int32_t *tri_vidx);
+c2a_status c2a_model_free(c2a_context *ctx, int32_t model_id);
+
+/* ---- queries (host buffers; synchronous) ------------------------------ */
+/* Runs n queries.  contacts may be NULL; else it must hold n x
+ * contacts_per_query records, of which only the first sum(min(num_contact,
+ * contacts_per_query)) are written, densely: query q's contacts start at
+ * results[q].contact_offset, in visiting order. */
+c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const c2a_params *params,
+                           c2a_result *results, c2a_contact *contacts);
+
+/* ---- queries (device buffers; asynchronous on stream) ----------------- */
+/* Same as c2a_solve_batch with every buffer in device memory, except that
+ * contacts stay in fixed slots: query q's at q * contacts_per_query.  stream
+ * is a cudaStream_t (NULL: the legacy default stream). */
+c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
+                                  const c2a_params *params, c2a_result *d_results, c2a_contact *d_contacts,
+                                  void *stream);
+
+/* One CA step per query (C2A_TimeOfContactStep) of the query's linear
+ * motions at time lambda[q]: lambda 0 uses the begin poses as given (the
+ * reference's first step), otherwise both motions are integrated to lambda.
+ * num_ca is the reference's res->numCA and prev_mint its res->mint before the
+ * step (the controlled error schedule reads both); the upper bound on the
+ * step is 1 - lambda.  Writes distance, mint, translation and the counters. */
+c2a_status c2a_toc_step_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *lambda,
+                              const int32_t *num_ca, const double *prev_mint, const c2a_params *params,
+                              c2a_result *results);
+
+/* Contact enumeration alone at fixed poses (C2A_QueryContactOnly):
+ * pose[0:12] = A, pose[24:36] = B; every triangle pair closer than
+ * threshold[q]. */
+c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *threshold,
+                                  int32_t contacts_per_query, c2a_result *results, c2a_contact *contacts);
+
+/* ---- motion (host) --------------------------------------------------- */
+/* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]
+ * angular speed, out[4:7] linear velocity, out[7:11] begin quaternion
+ * (x, y, z, w). */
+c2a_status c2a_motion_setup(const double *R0, const double *T0, const double *R1, const double *T1, double *out);
+/* Pose at time t (clamped to <= 1): R (9), T (3), qua (7: w, x, y, z, T). */
+c2a_status c2a_motion_integrate(const double *R0, const double *T0, const double *R1, const double *T1,
+                                double t, double *R, double *T, double *qua);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -101,6 +101,13 @@ int c2a_port_solve_batch(const c2a_port_model *models, int num_models, const int
                          const c2a_port_params *prm, c2a_port_result *res, c2a_port_contact *contacts,
                          int contacts_per_query, int num_threads);
 
+/* One CA step (C2A_TimeOfContactStep) of the query's motions at time lambda
+ * (0: the begin poses as given), with the schedule inputs num_ca and
+ * prev_mint; fills distance, mint, counters, translation and seeds. */
+int c2a_port_step(const c2a_port_model *A, const c2a_port_model *B, const double pose48[48], int seed_a,
+                  int seed_b, double lambda, int num_ca, double prev_mint, const c2a_port_params *prm,
+                  c2a_port_result *res);
+
 /* Contact enumeration alone (C2A_QueryContactOnly, C2A.cpp:1968-1983). */
 int c2a_port_contact_only(const c2a_port_model *A, const c2a_port_model *B,
                           const double Ra[9], const double Ta[3], const double Rb[9], const double Tb[3],

@@ -71,3 +71,9 @@ int c2a_port_solve_batch(const c2a_port_model *models, int num_models, const int
     if (num_threads == 0) worker(&j);
     return j.bad;
 }
+
+/* the deterministic sin/cos/acos the oracle uses, exported for the tests */
+#include "../c2a_gb300/csrc/common/c2a_detmath.h"
+double c2a_port_det_sin(double x) { return c2a_det_sin(x); }
+double c2a_port_det_cos(double x) { return c2a_det_cos(x); }
+double c2a_port_det_acos(double x) { return c2a_det_acos(x); }

@@ -745,3 +745,52 @@ int c2a_port_contact_only(const c2a_port_model *A, const c2a_port_model *B, cons
     contact_step(&st, (const double(*)[3])Ram, Ta, (const double(*)[3])Rbm, Tb, threshold);
     return st.num_contact;
 }
+
+int c2a_port_step(const c2a_port_model *A, const c2a_port_model *B, const double P[48], int seed_a, int seed_b,
+                  double lambda, int num_ca, double prev_mint, const c2a_port_params *prm, c2a_port_result *res)
+{
+    c2a_port_motion m1, m2;
+    step_state st;
+    double R1[3][3], T1[3], R2[3][3], T2[3];
+    int translation;
+    memset(res, 0, sizeof(*res));
+    if (seed_a < 0 || seed_a >= A->num_tris || seed_b < 0 || seed_b >= B->num_tris) return -1;
+    memset(&st, 0, sizeof(st));
+    c2a_port_motion_init(&m1, P, P + 9, P + 12, P + 21);
+    c2a_port_motion_init(&m2, P + 24, P + 33, P + 36, P + 45);
+    m1.toc_delta = prm->toc_delta;
+    m2.toc_delta = prm->toc_delta;
+    translation = (m1.angVel < 1e-8 && m2.angVel < 1e-8);
+    if (lambda != 0.0) {
+        double R19[9], R29[9];
+        c2a_port_motion_integrate(&m1, lambda, R19, T1, NULL);
+        c2a_port_motion_integrate(&m2, lambda, R29, T2, NULL);
+        pm_from9(R1, R19);
+        pm_from9(R2, R29);
+    } else {
+        pm_copy(R1, (const double(*)[3])m1.R);
+        pv_copy(T1, m1.T);
+        pm_copy(R2, (const double(*)[3])m2.R);
+        pv_copy(T2, m2.T);
+    }
+    st.o1 = A;
+    st.o2 = B;
+    st.m1 = &m1;
+    st.m2 = &m2;
+    st.seed_a = seed_a;
+    st.seed_b = seed_b;
+    st.numCA = num_ca;
+    st.mint = prev_mint;
+    st.UpboundTOC = 1.0 - lambda;
+    toc_step(&st, R1, T1, R2, T2, translation);
+    res->translation = translation;
+    res->numCA = num_ca;
+    res->toc = lambda;
+    res->distance = st.distance;
+    res->mint = st.mint;
+    res->num_bv_tests = st.num_bv_tests;
+    res->num_tri_tests = st.num_tri_tests;
+    res->seed_a = st.seed_a;
+    res->seed_b = st.seed_b;
+    return 0;
+}

@@ -1,0 +1,135 @@
+"""The library's host side without a GPU: its ABI surface, the RSS hierarchy
+build (bit-identical to the reference's EndModel) and the motion model."""
+import hashlib
+import os
+import re
+
+import numpy as np
+import pytest
+
+from c2a_testutil import GOLDEN, bits
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "c2a_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(c2a_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from c2a_gb300 import api
+
+    names = declared_symbols()
+    assert len(names) >= 14
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(api.ABI_SYMBOLS) == names
+
+
+def test_status_strings_and_host_only_context(lib):
+    from c2a_gb300 import api, meshes, workloads
+
+    assert api.status_str(0) == "ok"
+    assert "no CUDA device" in api.status_str(2)
+    with api.Context(-1) as ctx:
+        knot = meshes.torus_knot(2, 3, 12, 4)
+        mid = ctx.model(knot)
+        assert ctx.model_info(mid) == (96, 191, ctx.model_info(mid)[2])
+        qint = np.zeros((1, 4), dtype=np.int32)
+        poses = np.zeros((1, 48))
+        with pytest.raises(api.C2AError) as e:
+            ctx.solve(qint, poses, workloads.default_params(1.0, 1e-3, 40))
+        assert e.value.status == 2
+        ctx.free_model(mid)
+        with pytest.raises(api.C2AError):
+            ctx.model_info(mid)
+
+
+def test_empty_model_is_rejected(lib):
+    import ctypes as C
+    from c2a_gb300 import api
+
+    with api.Context(-1) as ctx:
+        mid = C.c_int32()
+        assert lib.c2a_model_build(ctx.h, 0, None, None, None, C.byref(mid)) == 5  # C2A_ERR_EMPTY_MODEL
+
+
+def _node_fields(ctx, mid):
+    f, fc, tv, tid, tidx = ctx.download(mid)
+    return f, fc, tv, tid, tidx
+
+
+def test_bvh_matches_reference_dump(lib):
+    from c2a_gb300 import api, meshes
+
+    z = np.load(f"{GOLDEN}/bvh_icosphere1_ref.npz")
+    m = meshes.Mesh("ico1", z["verts"], z["faces"], np.zeros((1, 3)), 0.0)
+    with api.Context(-1) as ctx:
+        f, fc, tv, tid, tidx = _node_fields(ctx, ctx.model(m))
+    assert bits(f) == bits(z["node_f"]) and np.array_equal(fc, z["first_child"])
+    assert bits(tv) == bits(z["tri_v"]) and np.array_equal(tid, z["tri_id"]) and np.array_equal(tidx, z["tri_idx"])
+
+
+@pytest.mark.parametrize("name", ["knot23_100x16", "knot35_60x12", "icosphere3", "soup2000", "knot23_400x50"])
+def test_bvh_matches_reference_hash(lib, name):
+    from c2a_gb300 import api, meshes
+
+    table = {l.split()[0]: l.split()[1:] for l in open(f"{GOLDEN}/bvh_hashes_ref.txt")}
+    bvh_hash, mesh_hash = table[name]
+    gen = {"knot23_100x16": lambda: meshes.torus_knot(2, 3, 100, 16),
+           "knot35_60x12": lambda: meshes.torus_knot(3, 5, 60, 12),
+           "icosphere3": lambda: meshes.icosphere(3, noise=0.02, seed=3),
+           "soup2000": lambda: meshes.triangle_soup(2000, seed=4),
+           "knot23_400x50": lambda: meshes.torus_knot(2, 3, 400, 50)}[name]
+    m = gen()
+    mh = hashlib.sha256(np.ascontiguousarray(m.verts).tobytes() + np.ascontiguousarray(m.faces).tobytes())
+    if mh.hexdigest() != mesh_hash:
+        pytest.skip("this platform's numpy generates a different mesh than the fixture's")
+    with api.Context(-1) as ctx:
+        arrays = _node_fields(ctx, ctx.model(m))
+    dig = hashlib.sha256()
+    for a in arrays:
+        dig.update(np.ascontiguousarray(a).tobytes())
+    assert dig.hexdigest() == bvh_hash
+
+
+def test_bvh_matches_port_on_degenerate_soups(lib, port):
+    """Degenerate triangles, repeated vertices, 1- and 2-triangle models."""
+    from c2a_gb300 import api, meshes
+
+    rng = np.random.default_rng(3)
+    cases = []
+    for n in (1, 2, 3, 7, 100):
+        v = rng.normal(size=(3 * n, 3))
+        f = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+        if n >= 3:
+            v[3] = v[4]  # a zero-length edge
+            v[6:9] = v[0]  # a triangle collapsed to a point
+        cases.append(meshes.Mesh(f"soup{n}", v, f, v, 0.0))
+    v = np.zeros((30, 3))
+    v[:, 0] = np.arange(30)  # all collinear
+    cases.append(meshes.Mesh("line", v, np.arange(30, dtype=np.int32).reshape(10, 3), v, 0.0))
+    with api.Context(-1) as ctx:
+        for m in cases:
+            f, fc, tv, tid, tidx = _node_fields(ctx, ctx.model(m))
+            nodes, tris = port.dump(port.models([m]), 0)
+            pf = np.concatenate([nodes["R"], nodes["Tr"], nodes["l"], nodes["r"][:, None], nodes["angR"][:, None],
+                                 nodes["Rloc"]], axis=1)
+            assert bits(f) == bits(pf), m.name
+            assert np.array_equal(fc, nodes["first_child"]), m.name
+            assert bits(tv) == bits(tris["v"]), m.name
+
+
+def test_motion_matches_reference(lib):
+    """CInterpMotion_Linear constants and integrate() (InterpMotion.cpp:228-287,
+    486-568) against the reference, bit for bit."""
+    from c2a_gb300 import api
+
+    z = np.load(f"{GOLDEN}/motion_ref.npz")
+    for i in range(len(z["t"])):
+        c = api.motion_setup(z["R0"][i], z["T0"][i], z["R1"][i], z["T1"][i])
+        assert bits(c[:7]) == bits(z["consts"][i]), i
+        R, T, qua = api.motion_integrate(z["R0"][i], z["T0"][i], z["R1"][i], z["T1"][i], z["t"][i])
+        assert bits(R) == bits(z["Rt"][i]) and bits(T) == bits(z["Tt"][i]), i

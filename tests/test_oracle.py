@@ -1,0 +1,120 @@
+"""The CPU oracle pinned against the reference.
+
+The reference has no tests and no stored outputs, so its known answers are
+produced by running the reference's own C2A sources (tests/golden/
+make_golden.py); these tests check the plain-C oracle port against those
+fixtures bit for bit, and against the live reference where it is compiled.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from c2a_testutil import GOLDEN, RESULT_FIELDS, bits, describe, load_fixture, result_mismatches
+
+
+@pytest.mark.parametrize("name", ["config1", "mixed", "translation"])
+def test_port_matches_reference_fixture(port, name):
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    models = port.models(ms)
+    res, con = port.solve_batch(models, qint, poses, params, threads=4, contacts_per_query=4096)
+    bad = result_mismatches(res, exp, con, econ, off)
+    assert not bad, f"{len(bad)} of {len(exp)} queries differ; first " + describe(res, exp, bad[0])
+
+
+def test_port_matches_shipped_c2a_solve(port):
+    """C2A_Solve as shipped: th_ca ignored, 1e-4 tolerances (C2A.cpp:2384-2388).
+    Its dres.mint is the contact query's reset value 1 when a contact was
+    found (C2A.cpp:1757), so mint is compared on collision-free queries only."""
+    ms, qint, poses, params, exp, econ, off = load_fixture("shipped_solve")
+    models = port.models(ms)
+    res, con = port.solve_batch(models, qint, poses, params, threads=4, contacts_per_query=4096)
+    fields = [f for f in RESULT_FIELDS if f != "mint"]
+    bad = result_mismatches(res, exp, con, econ, off, fields=fields)
+    assert not bad, describe(res, exp, bad[0])
+    free = exp["collisionfree"] == 1
+    assert bits(res["mint"][free]) == bits(exp["mint"][free])
+    assert np.all(exp["mint"][~free] == 1.0)
+
+
+def test_fixture_coverage():
+    """The fixtures exercise both outcomes, contacts, the translation-only CA,
+    several mesh families and non-default seeds."""
+    _, qint, _, _, exp, econ, _ = load_fixture("mixed")
+    assert 0 < exp["collisionfree"].sum() < len(exp)
+    assert len(econ) > 100 and set(np.unique(econ["type_a"])) >= {1, 2}
+    assert (qint[:, 2] != 0).any() and (qint[:, 1] == 1).any()
+    _, _, _, _, t, _, _ = load_fixture("translation")
+    assert t["translation"].all() and 0 < t["collisionfree"].sum() < len(t)
+
+
+def test_port_rect_and_triangle_distance(port):
+    z = np.load(f"{GOLDEN}/geometry_ref.npz")
+    for i in range(len(z["rect_d"])):
+        d, P, Q, S = port.rectdist(z["Rab"][i], z["Tab"][i], z["a"][i], z["b"][i])
+        assert bits(d) == bits(z["rect_d"][i]), i
+        if d > 0:
+            assert bits(S) == bits(z["rect_S"][i]), i
+    for i in range(len(z["tri_d"])):
+        d, P, Q, f = port.tridist(z["S9"][i], z["T9"][i])
+        assert bits(d) == bits(z["tri_d"][i]), i
+        assert f == tuple(int(x) for x in z["tri_f"][i]), i
+        if d > 0:
+            assert bits(P) == bits(z["tri_P"][i]) and bits(Q) == bits(z["tri_Q"][i]), i
+    assert (z["tri_d"] == 0).sum() > 5 and (z["rect_d"] == 0).sum() > 5
+
+
+def test_port_bvh_matches_reference(port):
+    from c2a_gb300 import meshes
+
+    z = np.load(f"{GOLDEN}/bvh_icosphere1_ref.npz")
+    m = meshes.Mesh("ico1", z["verts"], z["faces"], np.zeros((1, 3)), 0.0)
+    nodes, tris = port.dump(port.models([m]), 0)
+    f = np.concatenate([nodes["R"], nodes["Tr"], nodes["l"], nodes["r"][:, None], nodes["angR"][:, None],
+                        nodes["Rloc"]], axis=1)
+    assert bits(f) == bits(z["node_f"])
+    assert np.array_equal(nodes["first_child"], z["first_child"])
+    assert bits(tris["v"]) == bits(z["tri_v"]) and np.array_equal(tris["idx"], z["tri_idx"])
+
+
+def test_deterministic_math_is_correctly_rounded(port):
+    """sin/cos/acos of the motion model (InterpMotion.cpp:251, 275-278) against
+    200-bit mpmath: the double-double evaluation rounds correctly."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 200
+    L = port.lib
+    for fn in ("c2a_port_det_sin", "c2a_port_det_cos", "c2a_port_det_acos"):
+        getattr(L, fn).argtypes = [C.c_double]
+        getattr(L, fn).restype = C.c_double
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(0, np.pi / 2, 3000), [0.0, 1e-300, 1e-9, np.pi / 4, np.pi / 2]])
+    for x in xs:
+        assert L.c2a_port_det_sin(float(x)) == float(mpmath.sin(mpmath.mpf(float(x)))), x
+        assert L.c2a_port_det_cos(float(x)) == float(mpmath.cos(mpmath.mpf(float(x)))), x
+    ys = np.concatenate([rng.uniform(-1, 1, 3000), [-1.0, 1.0, 0.0, 1 - 2 ** -53, -1 + 2 ** -53]])
+    for y in ys:
+        assert L.c2a_port_det_acos(float(y)) == float(mpmath.acos(mpmath.mpf(float(y)))), y
+    assert np.isnan(L.c2a_port_det_acos(1.0000000000000002))
+
+
+def test_port_matches_live_reference(port, ref):
+    """Fresh random queries (random seed pairs, gaps down to contact) against
+    the reference compiled here."""
+    from c2a_gb300 import meshes, workloads
+    import contextlib, io
+
+    knot = meshes.torus_knot(3, 5, 40, 8)
+    qint, poses = workloads.ccd_queries(knot, knot, 48, 777, gap_range=(0.0, 0.8), device="cpu", model_a=0,
+                                        model_b=0)
+    rng = np.random.default_rng(5)
+    qint[:, 2] = rng.integers(0, knot.num_tris, len(qint))
+    qint[:, 3] = rng.integers(0, knot.num_tris, len(qint))
+    params = workloads.default_params(knot.bbox_diag(), 1e-3, 40)
+    res, con = port.solve_batch(port.models([knot]), qint, poses, params, contacts_per_query=4096)
+    h = ref.model(knot)
+    for q in range(len(qint)):
+        r, c = ref.solve(h, h, poses[q], int(qint[q, 2]), int(qint[q, 3]), params)
+        for f in RESULT_FIELDS:
+            assert bits(res[q][f]) == bits(r[f]), (q, f)
+        n = int(r["num_contact"])
+        assert bits(con[q][:n]) == bits(np.ascontiguousarray(c[::-1])), q
