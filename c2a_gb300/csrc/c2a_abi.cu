@@ -302,6 +302,41 @@ __global__ void c2a_gather_contacts(c2a_result *__restrict__ results, int n, int
     if (threadIdx.x == 0) results[q].contact_offset = off;
 }
 
+/* ------------------------------------------- scratch of the no-alloc entry */
+
+/* The solve kernel's scratch for c2a_solve_batch_noalloc: bytes [0, 4) hold
+ * the work counter, bytes [256, 256 + 32 * C2A_NOALLOC_MAX_MODELS) the model
+ * table.  Host code only ever sees the symbol's host-side stand-in; the
+ * device address comes from cudaGetSymbolAddress (noalloc_scratch below). */
+constexpr size_t kNoallocTableOffset = 256;
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[kNoallocTableOffset + sizeof(DevModel) * C2A_NOALLOC_MAX_MODELS];
+static_assert(sizeof(g_noalloc_scratch) == 4096, "the no-alloc scratch is documented as 4 KiB");
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char *g_noalloc_ptr[kMaxDevices] = {};
+
+/* device address of the scratch array on `device` (current), looked up once */
+c2a_status noalloc_scratch(int device, unsigned char **out)
+{
+    if (device < 0 || device >= kMaxDevices) return C2A_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        unsigned char *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            fprintf(stderr, "c2a_gb300: cudaGetSymbolAddress(no-alloc scratch) failed: %s\n", cudaGetErrorString(e));
+            return cuda_status(e == cudaSuccess ? cudaErrorInvalidSymbol : e);
+        }
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return C2A_OK;
+}
+} // namespace
+
 /* --------------------------------------------------------------- ABI */
 
 extern "C" {
@@ -318,6 +353,7 @@ const char *c2a_status_str(c2a_status s)
     case C2A_ERR_BAD_MODEL: return "unknown model id";
     case C2A_ERR_TREE_TOO_DEEP: return "hierarchy deeper than the traversal stack";
     case C2A_ERR_QUERY_FAILED: return "a query reported a non-zero status";
+    case C2A_ERR_NOALLOC_CAPACITY: return "more models than the no-alloc entry point's fixed table holds";
     default: return "unknown status";
     }
 }
@@ -537,6 +573,54 @@ c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n
     ctx->last_contacts = total;
     for (int32_t i = 0; i < n; i++)
         if (results[i].status & ~(C2A_QUERY_ITER_CAP | C2A_QUERY_CONTACT_OVERFLOW)) return C2A_ERR_QUERY_FAILED;
+    return C2A_OK;
+}
+
+c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
+                                   const c2a_params *params, c2a_result *d_results, c2a_contact *d_contacts,
+                                   void *stream)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    const size_t num_models = ctx->models.size();
+    if (num_models > C2A_NOALLOC_MAX_MODELS) {
+        fprintf(stderr,
+                "c2a_solve_batch_noalloc: the context holds %zu models; the fixed table of this entry point holds "
+                "at most %d\n",
+                num_models, C2A_NOALLOC_MAX_MODELS);
+        return C2A_ERR_NOALLOC_CAPACITY;
+    }
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    c2a_status st = check_depths(ctx);
+    if (st) return st;
+    unsigned char *scratch = nullptr;
+    st = noalloc_scratch(ctx->device, &scratch);
+    if (st) return st;
+    /* the model table on the stack, copied into the scratch array: no allocation on either side */
+    DevModel table[C2A_NOALLOC_MAX_MODELS];
+    for (size_t i = 0; i < num_models; i++) {
+        const ModelSlot &m = ctx->models[i];
+        table[i].nodes = m.d_nodes;
+        table[i].tris = m.d_tris;
+        table[i].num_tris = m.live ? (int32_t)m.host.tris.size() : 0;
+        table[i].num_nodes = m.live ? (int32_t)m.host.nodes.size() : 0;
+        table[i].depth = m.host.depth;
+        table[i].live = m.live ? 1 : 0;
+    }
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    DevModel *d_table = reinterpret_cast<DevModel *>(scratch + kNoallocTableOffset);
+    unsigned int *d_counter = reinterpret_cast<unsigned int *>(scratch);
+    if (num_models)
+        C2A_CUDA(cudaMemcpyAsync(d_table, table, sizeof(DevModel) * num_models, cudaMemcpyHostToDevice, s));
+    C2A_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s)); /* the last call left its count here */
+    c2a_params prm = *params;
+    if (!d_contacts) prm.contacts_per_query = 0;
+    c2a_solve_kernel<<<grid_for(ctx, n), kThreads, 0, s>>>(d_queries, n, d_table, (int)num_models, prm, d_results,
+                                                            d_contacts, d_counter);
+    ctx->launches++;
+    C2A_CUDA(cudaGetLastError());
+    /* the stack table is read by the copy engine before cudaMemcpyAsync returns (pageable source) */
     return C2A_OK;
 }
 

@@ -46,7 +46,8 @@ enum {
     C2A_ERR_EMPTY_MODEL = 5,      /* PQP_ERR_BUILD_EMPTY_MODEL (C2A_PQP.cpp:352-357) */
     C2A_ERR_BAD_MODEL = 6,        /* unknown or freed model id */
     C2A_ERR_TREE_TOO_DEEP = 7,    /* BVTT deeper than the traversal stack */
-    C2A_ERR_QUERY_FAILED = 8      /* at least one query has a non-zero status */
+    C2A_ERR_QUERY_FAILED = 8,     /* at least one query has a non-zero status */
+    C2A_ERR_NOALLOC_CAPACITY = 9  /* more models than c2a_solve_batch_noalloc's fixed table holds */
 };
 
 /* per-query status word (c2a_result.status), bit flags */
@@ -147,6 +148,28 @@ c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n
 c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
                                   const c2a_params *params, c2a_result *d_results, c2a_contact *d_contacts,
                                   void *stream);
+
+/* ---- queries without any device allocation --------------------------- */
+/* No counterpart in the reference.  For callers that may not allocate device
+ * memory at query time: code running under another allocator's fixed device
+ * budget (an engine or simulator that hands out its own buffers and forbids
+ * cudaMalloc after start-up), and real-time loops where cudaMalloc/cudaFree
+ * would stall on their implicit device synchronisation.  It does what
+ * c2a_solve_batch_device does (same kernel, same results, contacts in fixed
+ * slots), but the kernel's scratch -- the work counter and the table of model
+ * pointers -- lives in one file-scope device array of 4 KiB (room for
+ * C2A_NOALLOC_MAX_MODELS models) that every GPU loading the library holds
+ * until the process exits; no cudaMalloc, cudaFree or allocating library call
+ * is made.  The models must have been built with c2a_model_build beforehand
+ * (that call allocates).  The first call on a device looks up the array's
+ * device address, so make that first call before any stream capture.  Calls
+ * share the array: two calls whose kernels overlap on the GPU (different
+ * streams) race; serialise them.  More than C2A_NOALLOC_MAX_MODELS models in
+ * the context is rejected with C2A_ERR_NOALLOC_CAPACITY. */
+#define C2A_NOALLOC_MAX_MODELS 120
+c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
+                                   const c2a_params *params, c2a_result *d_results, c2a_contact *d_contacts,
+                                   void *stream);
 
 /* One CA step per query (C2A_TimeOfContactStep) of the query's linear
  * motions at time lambda[q]: lambda 0 uses the begin poses as given (the
