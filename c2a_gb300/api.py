@@ -79,11 +79,12 @@ def load(build_if_missing: bool = False) -> C.CDLL:
     global _LIB
     if _LIB is not None:
         return _LIB
-    if not os.path.exists(_build.LIB):
-        if not build_if_missing:
-            raise FileNotFoundError(f"{_build.LIB} is missing: run c2a_gb300.build.build() first")
+    path = os.environ.get("C2A_GB300_LIB") or _build.LIB  # a variant build (profiling) when set
+    if not os.path.exists(path):
+        if not build_if_missing or path != _build.LIB:
+            raise FileNotFoundError(f"{path} is missing: run c2a_gb300.build.build() first")
         _build.build()
-    lib = C.CDLL(_build.LIB)
+    lib = C.CDLL(path)
     vp, i32, dbl = C.c_void_p, C.c_int32, C.c_double
     sig = {
         "c2a_create": ([C.c_int, C.POINTER(vp)], i32),

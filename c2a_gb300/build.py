@@ -47,22 +47,30 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(s) <= t for s in _sources())
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
-    """Compiles every translation unit in parallel and links the shared library."""
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False, defines: tuple = (),
+          lib: str = LIB) -> str:
+    """Compiles every translation unit in parallel and links the shared library.
+
+    ``defines`` (e.g. ``("C2A_STATS",)`` for the event-counting profiling
+    build) and ``lib`` make a variant library elsewhere; the default is the
+    product library.
+    """
+    if not force and lib == LIB and not defines and up_to_date():
         return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
+    out_dir = os.path.dirname(os.path.abspath(lib))
+    os.makedirs(out_dir, exist_ok=True)
     nvcc = _nvcc()
+    dflags = [f"-D{d}" for d in defines]
     jobs = []
     for src in CUDA_SOURCES:
-        obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
-        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "--fmad=false", "-std=c++17", "-Xcompiler", HOST_FLAGS,
+        obj = os.path.join(out_dir, os.path.basename(src) + ".o")
+        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "--fmad=false", "-std=c++17", *dflags, "-Xcompiler", HOST_FLAGS,
                "-c", os.path.join(CSRC, src), "-o", obj]
         if ptxas_info:
             cmd.insert(1, "-Xptxas=-v")
         jobs.append((cmd, obj))
     for src in HOST_SOURCES:
-        obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src) + ".o")
         cmd = [nvcc, "-x", "c++", "-O2", "-std=c++17", "-Xcompiler", HOST_FLAGS, "-c", os.path.join(CSRC, src),
                "-o", obj]
         jobs.append((cmd, obj))
@@ -80,13 +88,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         logs = list(ex.map(run, jobs))
     if ptxas_info:
         print("\n".join(logs), file=sys.stderr)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     link = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp] + [o for _, o in jobs]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(link)}\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

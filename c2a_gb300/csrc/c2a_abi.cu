@@ -26,8 +26,37 @@ struct ModelSlot {
     BuiltModel host;
     NodeRec *d_nodes = nullptr;
     TriRec *d_tris = nullptr;
+    NodeShadow *d_snodes = nullptr;
+    TriShadow *d_stris = nullptr;
     bool live = false;
 };
+
+/* the kernels' view of one model slot */
+DevModel dev_model_of(const ModelSlot &s)
+{
+    DevModel m;
+    m.nodes = s.d_nodes;
+    m.tris = s.d_tris;
+    m.snodes = s.d_snodes;
+    m.stris = s.d_stris;
+    m.num_tris = s.live ? (int32_t)s.host.tris.size() : 0;
+    m.num_nodes = s.live ? (int32_t)s.host.nodes.size() : 0;
+    m.depth = s.host.depth;
+    m.flags = (s.live ? C2A_MODEL_LIVE : 0) | (s.live && s.host.shadow_ok ? C2A_MODEL_SHADOW_OK : 0);
+    return m;
+}
+
+void free_slot(ModelSlot &s)
+{
+    if (s.d_nodes) cudaFree(s.d_nodes);
+    if (s.d_tris) cudaFree(s.d_tris);
+    if (s.d_snodes) cudaFree(s.d_snodes);
+    if (s.d_stris) cudaFree(s.d_stris);
+    s.d_nodes = nullptr;
+    s.d_tris = nullptr;
+    s.d_snodes = nullptr;
+    s.d_stris = nullptr;
+}
 
 } // namespace
 
@@ -72,15 +101,7 @@ c2a_status sync_models(c2a_context *ctx)
 {
     if (!ctx->models_dirty) return C2A_OK;
     std::vector<DevModel> table(ctx->models.size());
-    for (size_t i = 0; i < ctx->models.size(); i++) {
-        const ModelSlot &s = ctx->models[i];
-        table[i].nodes = s.d_nodes;
-        table[i].tris = s.d_tris;
-        table[i].num_tris = s.live ? (int32_t)s.host.tris.size() : 0;
-        table[i].num_nodes = s.live ? (int32_t)s.host.nodes.size() : 0;
-        table[i].depth = s.host.depth;
-        table[i].live = s.live ? 1 : 0;
-    }
+    for (size_t i = 0; i < ctx->models.size(); i++) table[i] = dev_model_of(ctx->models[i]);
     if ((int)table.size() > ctx->d_models_cap) {
         if (ctx->d_models) cudaFree(ctx->d_models);
         ctx->d_models = nullptr;
@@ -123,11 +144,20 @@ c2a_status check_depths(c2a_context *ctx)
     return C2A_OK;
 }
 
-int grid_for(c2a_context *ctx, int n)
+/* launch shape of the persistent solve kernel: 128-thread blocks, or
+ * 32-thread blocks when the batch is too small to give every SM two full
+ * blocks (one query per thread, so small batches still reach all SMs) */
+struct Shape {
+    int blocks, threads;
+};
+Shape shape_for(c2a_context *ctx, int n)
 {
-    int blocks = ctx->sm_count * 8;
-    int need = (n + kThreads - 1) / kThreads;
-    return need < blocks ? (need > 0 ? need : 1) : blocks;
+    int threads = kThreads;
+    if ((n + kThreads - 1) / kThreads < 2 * ctx->sm_count) threads = 32;
+    const int most = ctx->sm_count * 8 * (kThreads / threads);
+    int need = (n + threads - 1) / threads;
+    if (need < 1) need = 1;
+    return Shape{need < most ? need : most, threads};
 }
 
 } // namespace
@@ -140,7 +170,7 @@ __global__ void __launch_bounds__(kThreads) c2a_solve_kernel(const c2a_query *__
                                                              c2a_contact *__restrict__ contacts,
                                                              unsigned int *__restrict__ counter)
 {
-    StackEntry stack[C2A_STACK_DEPTH];
+    Pending stack[C2A_STACK_DEPTH];
     for (;;) {
         const unsigned int q = atomicAdd(counter, 1u);
         if (q >= (unsigned int)n) break;
@@ -156,28 +186,28 @@ __global__ void __launch_bounds__(kThreads) c2a_step_kernel(const c2a_query *__r
                                                             const DevModel *__restrict__ models, int num_models,
                                                             c2a_params prm, c2a_result *__restrict__ results)
 {
-    StackEntry stack[C2A_STACK_DEPTH];
+    Pending stack[C2A_STACK_DEPTH];
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= n) return;
     const c2a_query &in = queries[qi];
     c2a_result &out = results[qi];
     out.status = 0;
     if (in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 || in.model_b >= num_models ||
-        !models[in.model_a].live || !models[in.model_b].live) {
+        !(models[in.model_a].flags & C2A_MODEL_LIVE) || !(models[in.model_b].flags & C2A_MODEL_LIVE)) {
         out.status = C2A_QUERY_BAD_INPUT;
         return;
     }
     Query q;
     q.A = models + in.model_a;
     q.B = models + in.model_b;
+    q.want_mint = true;
     if (in.seed_a < 0 || in.seed_a >= q.A->num_tris || in.seed_b < 0 || in.seed_b >= q.B->num_tris) {
         out.status = C2A_QUERY_BAD_INPUT;
         return;
     }
     q.status = 0;
     const double *P = in.pose;
-    motion_setup(q.m1, P, P + 9, P + 12, P + 21);
-    motion_setup(q.m2, P + 24, P + 33, P + 36, P + 45);
+    set_motions(q, P);
     q.toc_delta = prm.toc_delta;
     const bool translation = (q.m1.angVel < 1e-8 && q.m2.angVel < 1e-8);
     const double lam = lambda[qi];
@@ -193,8 +223,7 @@ __global__ void __launch_bounds__(kThreads) c2a_step_kernel(const c2a_query *__r
         motion_integrate(q.m1, lam, R1.m, &T1.x, orn);
         motion_integrate(q.m2, lam, R2.m, &T2.x, orn);
     }
-    q.r1 = R1;
-    q.t1 = T1;
+    set_pose1(q, R1, T1);
     q.seed_a = in.seed_a;
     q.seed_b = in.seed_b;
     q.nbv = q.ntri = 0;
@@ -202,6 +231,7 @@ __global__ void __launch_bounds__(kThreads) c2a_step_kernel(const c2a_query *__r
     q.mint = prev_mint[qi];
     q.upbound = 1.0 - lam;
     q.distance = 0;
+    q.abs_err = q.rel_err = 0;
     toc_step(q, R1, T1, R2, T2, translation, stack);
     out.collisionfree = 0;
     out.numCA = q.numCA;
@@ -223,7 +253,7 @@ __global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *
                                                                int slots, c2a_result *__restrict__ results,
                                                                c2a_contact *__restrict__ contacts)
 {
-    StackEntry stack[C2A_STACK_DEPTH];
+    Pending stack[C2A_STACK_DEPTH];
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= n) return;
     const c2a_query &in = queries[qi];
@@ -231,7 +261,7 @@ __global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *
     out.status = 0;
     out.num_contact = 0;
     if (in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 || in.model_b >= num_models ||
-        !models[in.model_a].live || !models[in.model_b].live) {
+        !(models[in.model_a].flags & C2A_MODEL_LIVE) || !(models[in.model_b].flags & C2A_MODEL_LIVE)) {
         out.status = C2A_QUERY_BAD_INPUT;
         return;
     }
@@ -239,10 +269,14 @@ __global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *
     q.A = models + in.model_a;
     q.B = models + in.model_b;
     q.status = 0;
+    q.want_mint = false; /* the contact recursion reads distances only */
+    q.e_ok = true;
+    q.nbv = q.ntri = 0;
     const double *P = in.pose;
     M3 R;
     V3 T;
     relative_transforms(q, pose_R(P), pose_T(P), pose_R(P + 24), pose_T(P + 24), R, T);
+    q.shadows_ok = q.e_ok && ((q.A->flags & q.B->flags) & C2A_MODEL_SHADOW_OK);
     const int cnt = contact_dfs(q, R, T, threshold[qi], stack,
                                 contacts ? contacts + (size_t)qi * (size_t)slots : nullptr, slots, qi);
     out.num_contact = cnt;
@@ -305,13 +339,14 @@ __global__ void c2a_gather_contacts(c2a_result *__restrict__ results, int n, int
 /* ------------------------------------------- scratch of the no-alloc entry */
 
 /* The solve kernel's scratch for c2a_solve_batch_noalloc: bytes [0, 4) hold
- * the work counter, bytes [256, 256 + 32 * C2A_NOALLOC_MAX_MODELS) the model
+ * the work counter, bytes [256, 256 + 48 * C2A_NOALLOC_MAX_MODELS) the model
  * table.  Host code only ever sees the symbol's host-side stand-in; the
  * device address comes from cudaGetSymbolAddress (noalloc_scratch below). */
 constexpr size_t kNoallocTableOffset = 256;
-static __device__ __align__(256) unsigned char
-    g_noalloc_scratch[kNoallocTableOffset + sizeof(DevModel) * C2A_NOALLOC_MAX_MODELS];
-static_assert(sizeof(g_noalloc_scratch) == 4096, "the no-alloc scratch is documented as 4 KiB");
+constexpr size_t kNoallocBytes = 8192;
+static_assert(kNoallocTableOffset + sizeof(DevModel) * C2A_NOALLOC_MAX_MODELS <= kNoallocBytes,
+              "the no-alloc model table must fit its 8 KiB scratch array");
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
 
 namespace {
 constexpr int kMaxDevices = 64;
@@ -396,10 +431,7 @@ c2a_status c2a_destroy(c2a_context *ctx)
     }
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (ModelSlot &s : ctx->models) {
-        if (s.d_nodes) cudaFree(s.d_nodes);
-        if (s.d_tris) cudaFree(s.d_tris);
-    }
+    for (ModelSlot &s : ctx->models) free_slot(s);
     if (ctx->d_models) cudaFree(ctx->d_models);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_buf) cudaFree(ctx->d_buf);
@@ -430,13 +462,30 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
         return C2A_OK;
     }
     C2A_CUDA(cudaSetDevice(ctx->device));
-    C2A_CUDA(cudaMalloc(&slot.d_nodes, sizeof(NodeRec) * slot.host.nodes.size()));
-    C2A_CUDA(cudaMalloc(&slot.d_tris, sizeof(TriRec) * slot.host.tris.size()));
-    C2A_CUDA(cudaMemcpyAsync(slot.d_nodes, slot.host.nodes.data(), sizeof(NodeRec) * slot.host.nodes.size(),
-                             cudaMemcpyHostToDevice, ctx->stream));
-    C2A_CUDA(cudaMemcpyAsync(slot.d_tris, slot.host.tris.data(), sizeof(TriRec) * slot.host.tris.size(),
-                             cudaMemcpyHostToDevice, ctx->stream));
-    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    const size_t nn = slot.host.nodes.size(), nt = slot.host.tris.size();
+    cudaError_t e = cudaMalloc(&slot.d_nodes, sizeof(NodeRec) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&slot.d_tris, sizeof(TriRec) * nt);
+    if (e == cudaSuccess) e = cudaMalloc(&slot.d_snodes, sizeof(NodeShadow) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&slot.d_stris, sizeof(TriShadow) * nt);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_nodes, slot.host.nodes.data(), sizeof(NodeRec) * nn, cudaMemcpyHostToDevice,
+                            ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_tris, slot.host.tris.data(), sizeof(TriRec) * nt, cudaMemcpyHostToDevice,
+                            ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_snodes, slot.host.snodes.data(), sizeof(NodeShadow) * nn,
+                            cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_stris, slot.host.stris.data(), sizeof(TriShadow) * nt, cudaMemcpyHostToDevice,
+                            ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        fprintf(stderr, "c2a_gb300: model upload failed: %s\n", cudaGetErrorString(e));
+        cudaStreamSynchronize(ctx->stream);
+        free_slot(slot);
+        return cuda_status(e);
+    }
     slot.live = true;
     ctx->models.push_back(std::move(slot));
     ctx->models_dirty = true;
@@ -494,11 +543,8 @@ c2a_status c2a_model_free(c2a_context *ctx, int32_t id)
     if (ctx->device >= 0) {
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
-        cudaFree(s.d_nodes);
-        cudaFree(s.d_tris);
+        free_slot(s);
     }
-    s.d_nodes = nullptr;
-    s.d_tris = nullptr;
     s.live = false;
     s.host = BuiltModel();
     ctx->models_dirty = true;
@@ -520,8 +566,9 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
     C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
     c2a_params prm = *params;
     if (!d_contacts) prm.contacts_per_query = 0;
-    c2a_solve_kernel<<<grid_for(ctx, n), kThreads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(),
-                                                            prm, d_results, d_contacts, ctx->d_counter);
+    const Shape sh = shape_for(ctx, n);
+    c2a_solve_kernel<<<sh.blocks, sh.threads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
+                                                       d_results, d_contacts, ctx->d_counter);
     ctx->launches++;
     C2A_CUDA(cudaGetLastError());
     return C2A_OK;
@@ -599,15 +646,7 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
     if (st) return st;
     /* the model table on the stack, copied into the scratch array: no allocation on either side */
     DevModel table[C2A_NOALLOC_MAX_MODELS];
-    for (size_t i = 0; i < num_models; i++) {
-        const ModelSlot &m = ctx->models[i];
-        table[i].nodes = m.d_nodes;
-        table[i].tris = m.d_tris;
-        table[i].num_tris = m.live ? (int32_t)m.host.tris.size() : 0;
-        table[i].num_nodes = m.live ? (int32_t)m.host.nodes.size() : 0;
-        table[i].depth = m.host.depth;
-        table[i].live = m.live ? 1 : 0;
-    }
+    for (size_t i = 0; i < num_models; i++) table[i] = dev_model_of(ctx->models[i]);
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     DevModel *d_table = reinterpret_cast<DevModel *>(scratch + kNoallocTableOffset);
     unsigned int *d_counter = reinterpret_cast<unsigned int *>(scratch);
@@ -616,8 +655,9 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
     C2A_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s)); /* the last call left its count here */
     c2a_params prm = *params;
     if (!d_contacts) prm.contacts_per_query = 0;
-    c2a_solve_kernel<<<grid_for(ctx, n), kThreads, 0, s>>>(d_queries, n, d_table, (int)num_models, prm, d_results,
-                                                            d_contacts, d_counter);
+    const Shape sh = shape_for(ctx, n);
+    c2a_solve_kernel<<<sh.blocks, sh.threads, 0, s>>>(d_queries, n, d_table, (int)num_models, prm, d_results,
+                                                       d_contacts, d_counter);
     ctx->launches++;
     C2A_CUDA(cudaGetLastError());
     /* the stack table is read by the copy engine before cudaMemcpyAsync returns (pageable source) */
@@ -700,6 +740,19 @@ c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, in
         if (results[i].status & ~C2A_QUERY_CONTACT_OVERFLOW) return C2A_ERR_QUERY_FAILED;
     return C2A_OK;
 }
+
+#ifdef C2A_STATS
+/* profiling builds only: copies the event counters out and clears them */
+c2a_status c2a_stats_read(unsigned long long *out, int count)
+{
+    if (!out || count < ST_COUNT) return C2A_ERR_INVALID_ARGUMENT;
+    C2A_CUDA(cudaDeviceSynchronize());
+    C2A_CUDA(cudaMemcpyFromSymbol(out, g_c2a_stats, sizeof(unsigned long long) * ST_COUNT));
+    unsigned long long zero[ST_COUNT] = {};
+    C2A_CUDA(cudaMemcpyToSymbol(g_c2a_stats, zero, sizeof(zero)));
+    return C2A_OK;
+}
+#endif
 
 c2a_status c2a_motion_setup(const double *R0, const double *T0, const double *R1, const double *T1, double *out)
 {

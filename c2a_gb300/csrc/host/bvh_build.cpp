@@ -19,6 +19,7 @@
  */
 #include "bvh_build.h"
 
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 
@@ -351,6 +352,16 @@ void jacobi_eigen3(double v[3][3], double d[3], const double a_in[3][3])
     d[2] = a[2][2];
 }
 
+namespace {
+/* FP32 rounding of an FP64 value; flags values outside FP32's normal range */
+float shadow_of(double x, bool &ok)
+{
+    const double a = std::fabs(x);
+    if (a != 0.0 && (a < (double)FLT_MIN || a > (double)FLT_MAX)) ok = false;
+    return (float)x;
+}
+} // namespace
+
 int build_rss_model(int32_t num_tris, const double *tv, const int32_t *ids, const int32_t *vidx, BuiltModel &out)
 {
     if (num_tris <= 0 || !tv) return C2A_ERR_EMPTY_MODEL;
@@ -398,6 +409,25 @@ int build_rss_model(int32_t num_tris, const double *tv, const int32_t *ids, cons
         t.id = tris[i].id;
         for (int k = 0; k < 3; k++) t.idx[k] = tris[i].idx[k];
     }
+    bool ok = true;
+    out.snodes.assign((size_t)num_nodes, NodeShadow{});
+    for (int32_t i = 0; i < num_nodes; i++) {
+        const NodeRec &n = out.nodes[i];
+        NodeShadow &s = out.snodes[i];
+        for (int k = 0; k < 9; k++) {
+            s.R[k] = shadow_of(n.R[k], ok);
+            s.Rloc[k] = shadow_of(n.Rloc[k], ok);
+        }
+        for (int k = 0; k < 3; k++) s.Tr[k] = shadow_of(n.Tr[k], ok);
+        s.l[0] = shadow_of(n.l[0], ok);
+        s.l[1] = shadow_of(n.l[1], ok);
+        s.r = shadow_of(n.r, ok);
+        s.angR = shadow_of(n.angR, ok);
+    }
+    out.stris.assign((size_t)num_tris, TriShadow{});
+    for (int32_t i = 0; i < num_tris; i++)
+        for (int k = 0; k < 9; k++) out.stris[i].v[k] = shadow_of(out.tris[i].v[k], ok);
+    out.shadow_ok = ok;
     return 0;
 }
 

@@ -41,10 +41,31 @@ struct alignas(16) TriRec {
 };
 static_assert(sizeof(TriRec) == 96, "triangle record must stay 96 bytes");
 
+/* FP32 shadows of the same records, rounded to nearest, for the kernels'
+ * certified FP32 filter (112 and 48 bytes). */
+struct alignas(16) NodeShadow {
+    float R[9];
+    float Tr[3];
+    float l[2];
+    float r;
+    float angR;
+    float Rloc[9];
+    float pad[3];
+};
+static_assert(sizeof(NodeShadow) == 112, "node shadow must stay 112 bytes");
+struct alignas(16) TriShadow {
+    float v[9];
+    float pad[3];
+};
+static_assert(sizeof(TriShadow) == 48, "triangle shadow must stay 48 bytes");
+
 struct BuiltModel {
     std::vector<NodeRec> nodes;
     std::vector<TriRec> tris;
-    int32_t depth = 0; /* maximum node depth (root = 0) */
+    std::vector<NodeShadow> snodes;
+    std::vector<TriShadow> stris;
+    bool shadow_ok = true; /* every shadowed value lies in FP32's normal range (or is 0) */
+    int32_t depth = 0;     /* maximum node depth (root = 0) */
 };
 
 /* C2A_Model::EndModel + C2A_BuildModel: returns 0 or a C2A_ERR_* code. */

@@ -157,7 +157,7 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
  * would stall on their implicit device synchronisation.  It does what
  * c2a_solve_batch_device does (same kernel, same results, contacts in fixed
  * slots), but the kernel's scratch -- the work counter and the table of model
- * pointers -- lives in one file-scope device array of 4 KiB (room for
+ * pointers -- lives in one file-scope device array of 8 KiB (room for
  * C2A_NOALLOC_MAX_MODELS models) that every GPU loading the library holds
  * until the process exits; no cudaMalloc, cudaFree or allocating library call
  * is made.  The models must have been built with c2a_model_build beforehand
