@@ -13,7 +13,7 @@
 #include <vector>
 
 #include "../../include/c2a_gb300.h"
-#include "device/ca_kernel.cuh"
+#include "device/ca_front.cuh"
 #include "host/bvh_build.h"
 
 using namespace c2a;
@@ -74,6 +74,10 @@ struct c2a_context {
     void *d_buf = nullptr;
     size_t d_buf_size = 0;
     int32_t last_contacts = 0; /* contacts copied back by the last c2a_solve_batch */
+    /* per-warp front slices of the canonical kernel (C2A_FRONT_CAP entries each) */
+    Pending *d_fronts = nullptr;
+    size_t fronts_warps = 0;
+    int canonical_blocks_per_sm = 0;
     std::mutex mu;
 };
 
@@ -131,7 +135,8 @@ c2a_status ensure_buf(c2a_context *ctx, size_t bytes)
 
 bool params_ok(const c2a_params *p)
 {
-    return p && p->max_iters >= 0 && p->contacts_per_query >= 0;
+    return p && p->max_iters >= 0 && p->contacts_per_query >= 0 &&
+           (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL);
 }
 
 /* queries must not pair models deeper than the traversal stack */
@@ -284,6 +289,30 @@ __global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *
     out.status = q.status | (cnt > slots ? C2A_QUERY_CONTACT_OVERFLOW : 0);
 }
 
+/* CANONICAL mode: one warp per query (persistent; warps take queries from
+ * the work counter), each with its own slice of the front buffer */
+__global__ void __launch_bounds__(kThreads) c2a_canonical_kernel(const c2a_query *__restrict__ queries, int n,
+                                                                 const DevModel *__restrict__ models,
+                                                                 int num_models, c2a_params prm,
+                                                                 c2a_result *__restrict__ results,
+                                                                 c2a_contact *__restrict__ contacts,
+                                                                 unsigned int *__restrict__ counter,
+                                                                 Pending *__restrict__ fronts)
+{
+    const int lane = threadIdx.x & 31;
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    Pending *stack = fronts + warp * (size_t)C2A_FRONT_CAP;
+    for (;;) {
+        unsigned int q = 0;
+        if (lane == 0) q = atomicAdd(counter, 1u);
+        q = __shfl_sync(kFullMask, q, 0);
+        if (q >= (unsigned int)n) break;
+        c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
+        solve_query_canonical(queries[q], models, num_models, prm, results[q], cq, stack, C2A_FRONT_CAP, lane,
+                              (int)q);
+    }
+}
+
 /* dense contact output: exclusive scan of min(num_contact, slots), then a
  * gather of the used slots (one block per 1024 queries, block-local scan
  * followed by a scan of the block totals) */
@@ -433,6 +462,7 @@ c2a_status c2a_destroy(c2a_context *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (ModelSlot &s : ctx->models) free_slot(s);
     if (ctx->d_models) cudaFree(ctx->d_models);
+    if (ctx->d_fronts) cudaFree(ctx->d_fronts);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_buf) cudaFree(ctx->d_buf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -563,9 +593,36 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
     st = sync_models(ctx);
     if (st) return st;
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
     c2a_params prm = *params;
     if (!d_contacts) prm.contacts_per_query = 0;
+    if (prm.mode == C2A_MODE_CANONICAL) {
+        if (!ctx->canonical_blocks_per_sm) {
+            int occ = 0;
+            C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_canonical_kernel, kThreads, 0));
+            ctx->canonical_blocks_per_sm = occ > 0 ? occ : 1;
+        }
+        const int most = ctx->sm_count * ctx->canonical_blocks_per_sm;
+        const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
+        const int blocks = need < most ? need : most;
+        const size_t warps = (size_t)blocks * (kThreads / 32);
+        if (warps > ctx->fronts_warps) {
+            /* a stream may still read the old slices: wait before freeing */
+            C2A_CUDA(cudaDeviceSynchronize());
+            if (ctx->d_fronts) cudaFree(ctx->d_fronts);
+            ctx->d_fronts = nullptr;
+            ctx->fronts_warps = 0;
+            const size_t want = (size_t)most * (kThreads / 32);
+            C2A_CUDA(cudaMalloc(&ctx->d_fronts, want * (size_t)C2A_FRONT_CAP * sizeof(Pending)));
+            ctx->fronts_warps = want;
+        }
+        C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
+        c2a_canonical_kernel<<<blocks, kThreads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
+                                                        d_results, d_contacts, ctx->d_counter, ctx->d_fronts);
+        ctx->launches++;
+        C2A_CUDA(cudaGetLastError());
+        return C2A_OK;
+    }
+    C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
     const Shape sh = shape_for(ctx, n);
     c2a_solve_kernel<<<sh.blocks, sh.threads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
                                                        d_results, d_contacts, ctx->d_counter);
@@ -630,6 +687,10 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
     if (n == 0) return C2A_OK;
+    if (params->mode != C2A_MODE_REFERENCE) {
+        fprintf(stderr, "c2a_solve_batch_noalloc: only C2A_MODE_REFERENCE runs without allocations\n");
+        return C2A_ERR_INVALID_ARGUMENT;
+    }
     const size_t num_models = ctx->models.size();
     if (num_models > C2A_NOALLOC_MAX_MODELS) {
         fprintf(stderr,
@@ -669,7 +730,8 @@ c2a_status c2a_toc_step_batch(c2a_context *ctx, const c2a_query *queries, int32_
                               c2a_result *results)
 {
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
-    if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!queries || !lambda || !num_ca || !prev_mint || !results)))
+    if (!ctx || n < 0 || !params_ok(params) || params->mode != C2A_MODE_REFERENCE ||
+        (n > 0 && (!queries || !lambda || !num_ca || !prev_mint || !results)))
         return C2A_ERR_INVALID_ARGUMENT;
     if (n == 0) return C2A_OK;
     std::lock_guard<std::mutex> lock(ctx->mu);

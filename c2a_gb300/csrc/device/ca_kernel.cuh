@@ -44,6 +44,7 @@ namespace c2a {
 enum {
     ST_EXPAND, ST_BVE, ST_BVE_FAIL, ST_BVE_ZERO, ST_EX_DESCEND, ST_EX_CONTRIB, ST_EX_ORDER, ST_LEAF,
     ST_LEAF_SKIP, ST_LEAF_EXACT, ST_LEAF_IMPROVE, ST_NO_SHADOW, ST_EXACT, ST_STEP, ST_CLEAF, ST_CLEAF_EXACT,
+    ST_D_ROUNDS, ST_D_POPS, ST_D_LEAF_EXACT, ST_D_KCYC, ST_T_ROUNDS, ST_T_POPS, ST_T_KCYC, ST_C_KCYC, ST_Q_KCYC,
     ST_COUNT
 };
 __device__ unsigned long long g_c2a_stats[ST_COUNT];
@@ -778,15 +779,15 @@ C2A_KNOINL void toc_step(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, bool translat
 
 /* --------------------------------------------------- contact enumeration */
 
-/* contacts of one leaf pair: written in visiting order; counted even when
- * the slots run out */
-C2A_KNOINL void contact_leaf(Query &q, int b1, int b2, double threshold, EF threshold_e, c2a_contact *out, int slots,
-                          int query_index, int &count)
+/* a leaf pair of the contact enumeration: true when its triangles lie within
+ * the threshold with valid features (C2A.cpp:1560-1630); fills c */
+C2A_KNOINL bool contact_leaf_test(Query &q, int b1, int b2, double threshold, EF threshold_e, int query_index,
+                                  c2a_contact &c)
 {
     const int ia = -q.A->nodes[b1].first_child - 1, ib = -q.B->nodes[b2].first_child - 1;
     C2A_STAT(q, ST_CLEAF);
     if (q.shadows_ok) {
-        EFCtx c{false};
+        EFCtx ec{false};
         V3T<EF> S[3], T[3], t[3];
         load_tri_e(S, q.A->stris + ia);
         load_tri_e(t, q.B->stris + ib);
@@ -796,36 +797,44 @@ C2A_KNOINL void contact_leaf(Query &q, int b1, int b2, double threshold, EF thre
         V3T<EF> p, qq;
         TriFeat f{-1, -1, -1, -1};
         bool col = false;
-        const EF d = tri_dist(p, qq, S, T, f, col, c);
-        if (!c.bad && f.type_a != -1 && f.type_b != -1 && ef_le3(d, threshold_e) == 0) return;
+        const EF d = tri_dist(p, qq, S, T, f, col, ec);
+        if (!ec.bad && f.type_a != -1 && f.type_b != -1 && ef_le3(d, threshold_e) == 0) return false;
     }
     C2A_STAT(q, ST_CLEAF_EXACT);
     V3 p, qq;
     TriFeat f{-1, -1, -1, -1};
     bool col = false;
     const double d = tri_distance_x(q, ia, ib, p, qq, f, col);
-    if (f.type_a == -1 || f.type_b == -1 || !(d <= threshold)) return;
-    if (count < slots && out) {
-        const TriRec *ta = q.A->tris + ia, *tb = q.B->tris + ib;
-        c2a_contact &c = out[count];
-        c.type_a = f.type_a + 1;
-        c.type_b = f.type_b + 1;
-        for (int k = 0; k < 3; k++) c.fid_a[k] = c.fid_b[k] = -1;
-        if (f.type_a == 0) c.fid_a[0] = ta->idx[f.fid_a];
-        if (f.type_a == 1) { c.fid_a[0] = ta->idx[f.fid_a]; c.fid_a[1] = ta->idx[(f.fid_a + 1) % 3]; }
-        if (f.type_a == 2) { c.fid_a[0] = ta->idx[0]; c.fid_a[1] = ta->idx[1]; c.fid_a[2] = ta->idx[2]; }
-        if (f.type_b == 0) c.fid_b[0] = tb->idx[f.fid_b];
-        if (f.type_b == 1) { c.fid_b[0] = tb->idx[f.fid_b]; c.fid_b[1] = tb->idx[(f.fid_b + 1) % 3]; }
-        if (f.type_b == 2) { c.fid_b[0] = tb->idx[0]; c.fid_b[1] = tb->idx[1]; c.fid_b[2] = tb->idx[2]; }
-        c.tri_a = ia;
-        c.tri_b = ib;
-        c.query = query_index;
-        c.pad = 0;
-        c.pa[0] = p.x; c.pa[1] = p.y; c.pa[2] = p.z;
-        const V3 pb = tmul(q.Rm, qq - q.Tm);
-        c.pb[0] = pb.x; c.pb[1] = pb.y; c.pb[2] = pb.z;
-        c.distance = d;
-    }
+    if (f.type_a == -1 || f.type_b == -1 || !(d <= threshold)) return false;
+    const TriRec *ta = q.A->tris + ia, *tb = q.B->tris + ib;
+    c.type_a = f.type_a + 1;
+    c.type_b = f.type_b + 1;
+    for (int k = 0; k < 3; k++) c.fid_a[k] = c.fid_b[k] = -1;
+    if (f.type_a == 0) c.fid_a[0] = ta->idx[f.fid_a];
+    if (f.type_a == 1) { c.fid_a[0] = ta->idx[f.fid_a]; c.fid_a[1] = ta->idx[(f.fid_a + 1) % 3]; }
+    if (f.type_a == 2) { c.fid_a[0] = ta->idx[0]; c.fid_a[1] = ta->idx[1]; c.fid_a[2] = ta->idx[2]; }
+    if (f.type_b == 0) c.fid_b[0] = tb->idx[f.fid_b];
+    if (f.type_b == 1) { c.fid_b[0] = tb->idx[f.fid_b]; c.fid_b[1] = tb->idx[(f.fid_b + 1) % 3]; }
+    if (f.type_b == 2) { c.fid_b[0] = tb->idx[0]; c.fid_b[1] = tb->idx[1]; c.fid_b[2] = tb->idx[2]; }
+    c.tri_a = ia;
+    c.tri_b = ib;
+    c.query = query_index;
+    c.pad = 0;
+    c.pa[0] = p.x; c.pa[1] = p.y; c.pa[2] = p.z;
+    const V3 pb = tmul(q.Rm, qq - q.Tm);
+    c.pb[0] = pb.x; c.pb[1] = pb.y; c.pb[2] = pb.z;
+    c.distance = d;
+    return true;
+}
+
+/* contacts of one leaf pair: written in visiting order; counted even when
+ * the slots run out */
+C2A_KDEV void contact_leaf(Query &q, int b1, int b2, double threshold, EF threshold_e, c2a_contact *out, int slots,
+                           int query_index, int &count)
+{
+    c2a_contact c;
+    if (!contact_leaf_test(q, b1, b2, threshold, threshold_e, query_index, c)) return;
+    if (count < slots && out) out[count] = c;
     count++;
 }
 

@@ -79,7 +79,21 @@ typedef struct c2a_params {
     int32_t max_iters;          /* CA iteration cap (reference: 150) */
     int32_t qsize;              /* front capacity hint; never changes a result */
     int32_t contacts_per_query; /* contact slots per query in the output buffer */
+    int32_t mode;               /* C2A_MODE_REFERENCE or C2A_MODE_CANONICAL */
+    int32_t reserved;           /* 0 */
 } c2a_params;
+
+/* C2A_MODE_REFERENCE: the reference's results bit for bit (its depth-first
+ * order; every step starts from the caller's seed pair, as C2A_Solve does).
+ * C2A_MODE_CANONICAL: before every rotation step, the reference's distance
+ * query (C2A_Distance with rel_err = abs_err = 0, C2A/src/C2A_PQP.cpp:971)
+ * finds the closest triangle pair and seeds the step with it, so each step's
+ * result is independent of traversal order; one warp runs each query over a
+ * parallel front.  Results equal that composition of the reference's own
+ * functions; contacts come sorted by (tri_a, tri_b), seed_a/seed_b are the
+ * last step's closest pair (ties: the smallest pair). */
+#define C2A_MODE_REFERENCE 0
+#define C2A_MODE_CANONICAL 1
 
 typedef struct c2a_result {
     int32_t collisionfree;

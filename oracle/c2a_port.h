@@ -58,7 +58,24 @@ typedef struct c2a_port_params {
     double contact_abs;  /* absolute term of the contact threshold (C2A.cpp:2433) */
     int with_contacts;   /* run the contact enumeration at the TOC */
     int max_iters;       /* CA iteration cap, 150 in the reference (C2A.cpp:2079) */
+    int mode;            /* C2A_PORT_MODE_REFERENCE or C2A_PORT_MODE_CANONICAL */
+    int reserved;
 } c2a_port_params;
+
+/* REFERENCE: every step starts from the caller's seed pair, as C2A_Solve does.
+ * CANONICAL: every step first finds the closest triangle pair with the
+ * reference's distance query (C2ADistanceRecurse, rel_err = abs_err = 0) and
+ * seeds the step with it, so the step's running bound starts at the exact
+ * minimum distance and its result no longer depends on the traversal order;
+ * contacts are sorted by (tri_a, tri_b). */
+enum { C2A_PORT_MODE_REFERENCE = 0, C2A_PORT_MODE_CANONICAL = 1 };
+
+/* The reference's distance query from a seed pair (C2A_Distance with
+ * rel_err = abs_err = 0, qsize <= 2; C2A/src/C2A_PQP.cpp:971-1056, 481-621):
+ * R/T place model B in model A; returns the minimum distance and the
+ * closest pair in *ta, *tb; counters in *nbv, *ntri (may be NULL). */
+double c2a_port_distance(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
+                         int seed_a, int seed_b, int *ta, int *tb, long long *nbv, long long *ntri);
 
 typedef struct c2a_port_contact {
     int type_a, type_b;  /* 1 vertex, 2 edge, 3 face (C2A.cpp:1584-1585) */

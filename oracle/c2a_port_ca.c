@@ -209,6 +209,7 @@ typedef struct step_state {
     long long num_bv_tests, num_tri_tests;
     int seed_a, seed_b;
     int numCA;
+    int canonical;        /* seed every rotation step with the closest pair */
     /* contact enumeration output */
     c2a_port_contact *contacts;
     int max_contacts, num_contact;
@@ -325,6 +326,96 @@ static void toc_recurse(step_state *st, const double R[3][3], const double T[3],
             else if (minta < st->mint) st->mint = minta;
         }
     }
+}
+
+/* ------------------------------------------------------- distance query */
+
+typedef struct dist_state {
+    const c2a_port_model *o1, *o2;
+    double R[3][3], T[3]; /* model 2 relative to model 1 */
+    double distance;
+    int t1, t2;
+    long long num_bv_tests, num_tri_tests;
+} dist_state;
+
+/* C2ADistanceRecurse, C2A/src/C2A_PQP.cpp:481-621, with rel_err = abs_err = 0 */
+static void dist_recurse(dist_state *ds, const double R[3][3], const double T[3], int b1, int b2)
+{
+    const c2a_port_node *n1 = &ds->o1->nodes[b1], *n2 = &ds->o2->nodes[b2];
+    int l1 = n1->first_child < 0, l2 = n2->first_child < 0;
+    if (l1 && l2) {
+        double p[3], q[3], d;
+        int ia = -n1->first_child - 1, ib = -n2->first_child - 1;
+        ds->num_tri_tests++;
+        d = tri_distance_plain((const double(*)[3])ds->R, ds->T, &ds->o1->tris[ia], &ds->o2->tris[ib], p, q);
+        if (d < ds->distance) {
+            ds->distance = d;
+            ds->t1 = ia;
+            ds->t2 = ib;
+        }
+        return;
+    }
+    {
+        int a1, a2, c1, c2;
+        double R1[3][3], T1[3], R2[3][3], T2[3], S[3], d1, d2;
+        step_state cs;
+        cs.o1 = ds->o1;
+        cs.o2 = ds->o2;
+        children(&cs, b1, b2, R, T, &a1, &a2, &c1, &c2, R1, T1, R2, T2);
+        ds->num_bv_tests += 2;
+        d1 = bv_distance((const double(*)[3])R1, T1, &ds->o1->nodes[a1], &ds->o2->nodes[a2], S);
+        d2 = bv_distance((const double(*)[3])R2, T2, &ds->o1->nodes[c1], &ds->o2->nodes[c2], S);
+        if (d2 < d1) {
+            if ((d2 < (ds->distance - 0)) || (d2 * (1 + 0) < ds->distance))
+                dist_recurse(ds, (const double(*)[3])R2, T2, c1, c2);
+            if ((d1 < (ds->distance - 0)) || (d1 * (1 + 0) < ds->distance))
+                dist_recurse(ds, (const double(*)[3])R1, T1, a1, a2);
+        } else {
+            if ((d1 < (ds->distance - 0)) || (d1 * (1 + 0) < ds->distance))
+                dist_recurse(ds, (const double(*)[3])R1, T1, a1, a2);
+            if ((d2 < (ds->distance - 0)) || (d2 * (1 + 0) < ds->distance))
+                dist_recurse(ds, (const double(*)[3])R2, T2, c1, c2);
+        }
+    }
+}
+
+/* C2A_Distance (C2A_PQP.cpp:971-1056): initial bound from the seed pair, then
+ * the recursion from the two root nodes */
+static double distance_query(const c2a_port_model *A, const c2a_port_model *B, const double Rm[3][3],
+                             const double Tm[3], int seed_a, int seed_b, int *ta, int *tb, long long *nbv,
+                             long long *ntri)
+{
+    dist_state ds;
+    double p[3], q[3], Rtemp[3][3], R[3][3], Ttemp[3], T[3];
+    const c2a_port_node *r1 = &A->nodes[0], *r2 = &B->nodes[0];
+    ds.o1 = A;
+    ds.o2 = B;
+    pm_copy(ds.R, Rm);
+    pv_copy(ds.T, Tm);
+    ds.distance = tri_distance_plain(Rm, Tm, &A->tris[seed_a], &B->tris[seed_b], p, q);
+    ds.t1 = seed_a;
+    ds.t2 = seed_b;
+    ds.num_bv_tests = 0;
+    ds.num_tri_tests = 0;
+    pm_mul(Rtemp, Rm, (const double(*)[3])r2->R);
+    pm_tmul(R, (const double(*)[3])r1->R, (const double(*)[3])Rtemp);
+    pm_mul_v_add(Ttemp, Rm, r2->Tr, Tm);
+    pv_sub(Ttemp, Ttemp, r1->Tr);
+    pm_tmul_v(T, (const double(*)[3])r1->R, Ttemp);
+    dist_recurse(&ds, (const double(*)[3])R, T, 0, 0);
+    *ta = ds.t1;
+    *tb = ds.t2;
+    if (nbv) *nbv = ds.num_bv_tests;
+    if (ntri) *ntri = ds.num_tri_tests;
+    return ds.distance;
+}
+
+double c2a_port_distance(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
+                         int seed_a, int seed_b, int *ta, int *tb, long long *nbv, long long *ntri)
+{
+    double Rm[3][3];
+    pm_from9(Rm, R);
+    return distance_query(A, B, (const double(*)[3])Rm, T, seed_a, seed_b, ta, tb, nbv, ntri);
 }
 
 /* -------------------------------------------------- translation-only CA */
@@ -518,6 +609,15 @@ static void toc_step(step_state *st, double R1[3][3], double T1[3], double R2[3]
         }
         return;
     }
+    if (st->canonical) {
+        /* the closest pair becomes the step's seed (C2A_Distance, then
+         * res->last_triA/B := that pair, then C2A_TimeOfContactStep) */
+        int ta, tb;
+        distance_query(st->o1, st->o2, (const double(*)[3])st->R, st->T, st->seed_a, st->seed_b, &ta, &tb, NULL,
+                       NULL);
+        st->seed_a = ta;
+        st->seed_b = tb;
+    }
     st->distance = tri_distance_plain((const double(*)[3])st->R, st->T, &st->o1->tris[st->seed_a],
                                       &st->o2->tris[st->seed_b], p, q);
     if (st->numCA == 0) st->mint = 1;
@@ -592,6 +692,15 @@ static void contact_recurse(step_state *st, const double R[3][3], const double T
                 contact_recurse(st, (const double(*)[3])R2, T2, c1, c2);
         }
     }
+}
+
+/* canonical contact order: by post-build triangle pair */
+static int contact_cmp(const void *a, const void *b)
+{
+    const c2a_port_contact *x = (const c2a_port_contact *)a, *y = (const c2a_port_contact *)b;
+    if (x->tri_a != y->tri_a) return x->tri_a < y->tri_a ? -1 : 1;
+    if (x->tri_b != y->tri_b) return x->tri_b < y->tri_b ? -1 : 1;
+    return 0;
 }
 
 /* C2A_TimeOfContactStep_Contact, C2A.cpp:1727-1775 */
@@ -694,6 +803,7 @@ int c2a_port_solve(const c2a_port_model *A, const c2a_port_model *B, const doubl
     st.m2 = &m2;
     st.seed_a = seed_a;
     st.seed_b = seed_b;
+    st.canonical = (prm->mode == C2A_PORT_MODE_CANONICAL);
     toc = query_toc(&st, prm, translation, &cf);
     res->translation = translation;
     res->collisionfree = cf;
@@ -724,6 +834,10 @@ int c2a_port_solve(const c2a_port_model *A, const c2a_port_model *B, const doubl
             st.UpboundTOC = 1;
             contact_step(&st, (const double(*)[3])Ram, Ta, (const double(*)[3])Rbm, Tb, threshold);
             res->num_contact = st.num_contact;
+            if (st.canonical && contacts) {
+                const int kept = st.num_contact < st.max_contacts ? st.num_contact : st.max_contacts;
+                qsort(contacts, (size_t)kept, sizeof(c2a_port_contact), contact_cmp);
+            }
         }
     }
     return 0;
@@ -782,6 +896,7 @@ int c2a_port_step(const c2a_port_model *A, const c2a_port_model *B, const double
     st.numCA = num_ca;
     st.mint = prev_mint;
     st.UpboundTOC = 1.0 - lambda;
+    st.canonical = (prm->mode == C2A_PORT_MODE_CANONICAL);
     toc_step(&st, R1, T1, R2, T2, translation);
     res->translation = translation;
     res->numCA = num_ca;

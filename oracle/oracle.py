@@ -43,7 +43,10 @@ def build(ref: bool | None = None) -> None:
 
 class _Params(C.Structure):
     _fields_ = [("tol_d", C.c_double), ("tol_t", C.c_double), ("toc_delta", C.c_double),
-                ("contact_abs", C.c_double), ("with_contacts", C.c_int), ("max_iters", C.c_int)]
+                ("contact_abs", C.c_double), ("with_contacts", C.c_int), ("max_iters", C.c_int),
+                ("mode", C.c_int), ("reserved", C.c_int)]
+
+MODE_REFERENCE, MODE_CANONICAL = 0, 1
 
 
 class _PortModel(C.Structure):
@@ -58,7 +61,7 @@ TRI_DTYPE = np.dtype([("v", np.float64, (9,)), ("id", np.int32), ("idx", np.int3
 
 def _params(p: dict) -> _Params:
     return _Params(float(p["tol_d"]), float(p["tol_t"]), float(p["toc_delta"]), float(p["contact_abs"]),
-                   int(p.get("with_contacts", 1)), int(p.get("max_iters", 150)))
+                   int(p.get("with_contacts", 1)), int(p.get("max_iters", 150)), int(p.get("mode", 0)), 0)
 
 
 def _dptr(a):
@@ -152,6 +155,7 @@ class Ref:
         L.c2a_ref_model_dump.argtypes = [C.c_void_p] * 6
         L.c2a_ref_solve.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 8 + [C.c_int, C.c_int] + \
                                    [C.c_double] * 4 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        L.c2a_ref_solve_canonical.argtypes = L.c2a_ref_solve.argtypes
         L.c2a_ref_solve_shipped.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 8 + [C.c_int, C.c_int] + \
                                            [C.c_void_p, C.c_void_p, C.c_int]
         L.c2a_ref_rectdist.argtypes = [C.c_void_p] * 7
@@ -192,7 +196,8 @@ class Ref:
         if shipped:
             self.lib.c2a_ref_solve_shipped(ha, hb, *ptrs, seed_a, seed_b, _dptr(res), _dptr(con), max_contacts)
         else:
-            self.lib.c2a_ref_solve(ha, hb, *ptrs, seed_a, seed_b, float(params["tol_d"]), float(params["tol_t"]),
+            fn = self.lib.c2a_ref_solve_canonical if params.get("mode", 0) == MODE_CANONICAL else self.lib.c2a_ref_solve
+            fn(ha, hb, *ptrs, seed_a, seed_b, float(params["tol_d"]), float(params["tol_t"]),
                                    float(params["toc_delta"]), float(params["contact_abs"]),
                                    int(params.get("with_contacts", 1)), int(params.get("max_iters", 150)),
                                    _dptr(res), _dptr(con), max_contacts)

@@ -12,6 +12,7 @@
 #include <string>
 #include <list>
 #include <vector>
+#include <algorithm>
 #include <iostream>
 #include "PQP.h"
 #include "MatVec.h"
@@ -24,6 +25,11 @@ extern bool b_TanslationCCD; // C2A/src/C2A.cpp:33
 
 PQP_REAL TriDist(PQP_REAL P[3], PQP_REAL Q[3], const PQP_REAL S[3][3], const PQP_REAL T[3][3],
                  C2A_ContactFeature &f1, C2A_ContactFeature &f2, bool &bCollided);
+
+// defined in C2A/src/C2A.cpp:1778-1789, not declared in its headers
+int C2A_TimeOfContactStep(CInterpMotion *objmotion1, CInterpMotion *objmotion2, C2A_TimeOfContactResult *res,
+                          PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3], PQP_REAL T2[3],
+                          C2A_Model *o2, PQP_REAL tolerance_t, PQP_REAL tolerance_d);
 
 extern "C" {
 
@@ -180,6 +186,152 @@ int c2a_ref_solve(void *ha, void *hb, const double *R0a, const double *T0a, cons
       C2A_QueryContact(&motion1, &motion2, &dres, A, B, threshold);
       out->num_contact = dres.num_contact;
       copy_contacts(dres, contacts, max_contacts);
+    }
+  }
+  return 0;
+}
+
+// CANONICAL composition of the reference's own functions: before every
+// rotation step, C2A_Distance (rel_err = abs_err = 0, qsize 2; C2A_PQP.cpp:971)
+// from the current seed pair finds the closest triangle pair, which then seeds
+// C2A_TimeOfContactStep (res->last_triA/B).  The loop around the steps is a
+// harness copy of C2A_QueryTimeOfContact's (C2A.cpp:1987-2146) so the
+// distance query can run between steps; contacts are sorted by (tri_a, tri_b).
+static void closest_seed(C2A_TimeOfContactResult &dres, C2A_Model *A, C2A_Model *B, PQP_REAL R1[3][3],
+                         PQP_REAL T1[3], PQP_REAL R2[3][3], PQP_REAL T2[3])
+{
+  C2A_DistanceResult dd;
+  A->last_tri = dres.last_triA;
+  B->last_tri = dres.last_triB;
+  C2A_Distance(&dd, R1, T1, A, R2, T2, B, 0.0, 0.0, 2);
+  dres.last_triA = A->last_tri;
+  dres.last_triB = B->last_tri;
+}
+
+// C2A_Distance (rel_err = abs_err = 0, qsize 2) from a seed pair; R/T place
+// model B in model A's frame.  Returns the distance; *ta/*tb the closest pair.
+double c2a_ref_distance(void *ha, void *hb, const double *R9, const double *T3, int seed_a, int seed_b, int *ta,
+                        int *tb, long long *nbv, long long *ntri)
+{
+  C2A_Model *A = (C2A_Model *)ha, *B = (C2A_Model *)hb;
+  PQP_REAL I[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, Z[3] = {0, 0, 0}, R[3][3], T[3];
+  m9(R, R9);
+  VcV(T, T3);
+  C2A_DistanceResult dd;
+  A->last_tri = A->GetTriangle(seed_a);
+  B->last_tri = B->GetTriangle(seed_b);
+  C2A_Distance(&dd, I, Z, A, R, T, B, 0.0, 0.0, 2);
+  *ta = tri_index(A, A->last_tri);
+  *tb = tri_index(B, B->last_tri);
+  if (nbv) *nbv = dd.num_bv_tests;
+  if (ntri) *ntri = dd.num_tri_tests;
+  return dd.distance;
+}
+
+int c2a_ref_solve_canonical(void *ha, void *hb, const double *R0a, const double *T0a, const double *R1a,
+                            const double *T1a, const double *R0b, const double *T0b, const double *R1b,
+                            const double *T1b, int seed_a, int seed_b, double tol_d, double tol_t,
+                            double toc_delta, double contact_abs, int with_contacts, int max_iters,
+                            ref_result *out, ref_contact *contacts, int max_contacts)
+{
+  C2A_Model *A = (C2A_Model *)ha, *B = (C2A_Model *)hb;
+  PQP_REAL R1[3][3], T1[3], R2[3][3], T2[3], R1e[3][3], T1e[3], R2e[3][3], T2e[3];
+  m9(R1, R0a); VcV(T1, T0a); m9(R1e, R1a); VcV(T1e, T1a);
+  m9(R2, R0b); VcV(T2, T0b); m9(R2e, R1b); VcV(T2e, T1b);
+  CInterpMotion_Linear motion1(R1, T1, R1e, T1e);
+  CInterpMotion_Linear motion2(R2, T2, R2e, T2e);
+  motion1.m_toc_delta = toc_delta;
+  motion2.m_toc_delta = toc_delta;
+  b_TanslationCCD = (motion1.m_angVel < 1e-8 && motion2.m_angVel < 1e-8);
+  C2A_TimeOfContactResult dres;
+  dres.last_triA = A->GetTriangle(seed_a);
+  dres.last_triB = B->GetTriangle(seed_b);
+  dres.num_contact = 0;
+  dres.num_bv_tests = 0;
+  dres.num_tri_tests = 0;
+  dres.UpboundTOC = 1;
+  dres.numCA = 0;
+  motion1.transform.Rotation().Get_Value(R1);
+  motion1.transform.Translation().Get_Value(T1);
+  motion2.transform.Rotation().Get_Value(R2);
+  motion2.transform.Translation().Get_Value(T2);
+  PQP_REAL lamda = 0.0, lastLamda = 0, dlamda = 0.0, toc = 0;
+  bool collisionfree = false, done = false;
+  if (!b_TanslationCCD) closest_seed(dres, A, B, R1, T1, R2, T2);
+  C2A_TimeOfContactStep(&motion1, &motion2, &dres, R1, T1, A, R2, T2, B, tol_t, tol_d);
+  PQP_REAL dist = dres.distance, mint = dres.mint;
+  if (b_TanslationCCD) {
+    collisionfree = (mint >= 1.0);
+    toc = mint;
+    done = true;
+  } else {
+    dres.numCA = 1;
+    lastLamda = mint;
+    int nItrs = 0;
+    while (dist > tol_d) {
+      if (++nItrs > max_iters) break;
+      if (mint >= 1.0) { collisionfree = true; toc = 0; done = true; break; }
+      dlamda = mint;
+      if (dlamda < tol_t) break;
+      lamda += dlamda;
+      if (lamda >= 1.0) { collisionfree = true; toc = 0; done = true; break; }
+      lastLamda = lamda;
+      dres.numCA++;
+      ((CInterpMotion *)&motion1)->integrate(lamda, R1, T1); /* the base-class overload */
+      ((CInterpMotion *)&motion2)->integrate(lamda, R2, T2);
+      dres.UpboundTOC = 1.0 - lamda;
+      closest_seed(dres, A, B, R1, T1, R2, T2);
+      C2A_TimeOfContactStep(&motion1, &motion2, &dres, R1, T1, A, R2, T2, B, tol_t, tol_d);
+      dist = dres.distance;
+      mint = dres.mint;
+    }
+  }
+  if (!done) {
+    toc = (dist == 0 && mint < 0) ? lastLamda - dlamda : lastLamda;
+    collisionfree = false;
+    if (toc >= 1 - tol_t) toc = 0;
+  }
+  memset(out, 0, sizeof(*out));
+  out->translation = b_TanslationCCD ? 1 : 0;
+  out->collisionfree = collisionfree ? 1 : 0;
+  out->toc = toc;
+  out->numCA = dres.numCA;
+  out->distance = dres.distance;
+  out->mint = dres.mint;
+  out->num_bv_tests = dres.num_bv_tests;
+  out->num_tri_tests = dres.num_tri_tests;
+  out->seed_a = tri_index(A, dres.last_triA);
+  out->seed_b = tri_index(B, dres.last_triB);
+  dres.cont_l.clear();
+  if (!collisionfree) {
+    PQP_REAL qua[7], R[3][3], T[3];
+    motion1.integrate(toc, qua);
+    motion1.transform.Rotation().Get_Value(R);
+    motion1.transform.Translation().Get_Value(T);
+    for (int i = 0; i < 3; i++) {
+      for (int j = 0; j < 3; j++) out->R_toc[0][3 * i + j] = R[i][j];
+      out->T_toc[0][i] = T[i];
+    }
+    motion2.integrate(toc, qua);
+    motion2.transform.Rotation().Get_Value(R);
+    motion2.transform.Translation().Get_Value(T);
+    for (int i = 0; i < 3; i++) {
+      for (int j = 0; j < 3; j++) out->R_toc[1][3 * i + j] = R[i][j];
+      out->T_toc[1][i] = T[i];
+    }
+    if (with_contacts) {
+      double threshold = 2 * dres.distance + contact_abs;
+      C2A_QueryContact(&motion1, &motion2, &dres, A, B, threshold);
+      out->num_contact = dres.num_contact;
+      int kept = copy_contacts(dres, contacts, max_contacts);
+      if (contacts) {
+        if (kept > max_contacts) kept = max_contacts;
+        std::vector<ref_contact> v(contacts, contacts + kept);
+        std::sort(v.begin(), v.end(), [](const ref_contact &x, const ref_contact &y) {
+          return x.tri_a != y.tri_a ? x.tri_a < y.tri_a : x.tri_b < y.tri_b;
+        });
+        std::copy(v.begin(), v.end(), contacts);
+      }
     }
   }
   return 0;

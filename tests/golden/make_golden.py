@@ -2,7 +2,8 @@
 
 Run where the reference is compiled (``make -C oracle ref``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py canonical  # the canonical-mode ones only
 
 Each fixture stores its inputs (mesh vertices and faces, query poses and
 seeds, parameters) together with what the reference computed, so checking it
@@ -47,17 +48,22 @@ def quiet_stdout():
             os.close(fd)
 
 
-def run_ref(ref, handles, wl, shipped=False, max_contacts=4096):
+def run_ref(ref, handles, wl, shipped=False, max_contacts=4096, handles_b=None):
+    """handles_b: separate model objects for side B (the canonical composition
+    needs them: C2A_Distance records its closest pair in each model's last_tri)."""
     res = np.zeros(wl.n, dtype=RESULT_DTYPE)
     cons, offs = [], [0]
+    canonical = wl.params.get("mode", 0) == 1
+    hb = handles if handles_b is None else handles_b
     with quiet_stdout():
         for q in range(wl.n):
             ma, mb, sa, sb = (int(x) for x in wl.qint[q])
-            r, c = ref.solve(handles[ma], handles[mb], wl.poses[q], sa, sb, wl.params, max_contacts=max_contacts,
+            r, c = ref.solve(handles[ma], hb[mb], wl.poses[q], sa, sb, wl.params, max_contacts=max_contacts,
                              shipped=shipped)
             res[q] = r
             # the reference's list is push_front: store in visiting order
-            cons.append(np.ascontiguousarray(c[::-1]))
+            # (the canonical composition returns them sorted by triangle pair)
+            cons.append(np.ascontiguousarray(c if canonical else c[::-1]))
             offs.append(offs[-1] + len(c))
     con = np.concatenate(cons) if offs[-1] else np.zeros(0, dtype=CONTACT_DTYPE)
     return res, con, np.array(offs, dtype=np.int64)
@@ -189,9 +195,40 @@ def bvh_hashes(ref):
     print("bvh hashes:", out)
 
 
+def canonical_fixtures(ref):
+    """The CANONICAL composition of the reference's own functions: C2A_Distance
+    (rel_err = abs_err = 0) seeds every rotation step with the closest pair."""
+    wl = workloads.config1(n=64, seed=201, device="cpu")
+    wl.params["mode"] = 1
+    with quiet_stdout():
+        hs = [ref.model(m) for m in wl.meshes]
+        hb = [ref.model(m) for m in wl.meshes]
+    save_workload("canonical_config1_ref.npz", wl, *run_ref(ref, hs, wl, handles_b=hb))
+
+    knot = meshes.torus_knot(2, 3, 24, 6)
+    ico = meshes.icosphere(2, radius=0.8, noise=0.02, seed=7)
+    qa, pa = workloads.ccd_queries(knot, knot, 48, 202, gap_range=(0.0, 0.6), device="cpu", model_a=0, model_b=0)
+    qb, pb = workloads.ccd_queries(knot, ico, 48, 203, gap_range=(0.02, 0.6), device="cpu", model_a=0, model_b=1)
+    rng = np.random.default_rng(204)
+    qa[:, 2] = rng.integers(0, knot.num_tris, len(qa))
+    qa[:, 3] = rng.integers(0, knot.num_tris, len(qa))
+    qb[:, 2] = rng.integers(0, knot.num_tris, len(qb))
+    qb[:, 3] = rng.integers(0, ico.num_tris, len(qb))
+    wl2 = workloads.Workload("canonical_mixed", [knot, ico], np.concatenate([qa, qb]), np.concatenate([pa, pb]),
+                             workloads.default_params(knot.bbox_diag(), 1e-3, 40))
+    wl2.params["mode"] = 1
+    with quiet_stdout():
+        hs = [ref.model(m) for m in wl2.meshes]
+        hb = [ref.model(m) for m in wl2.meshes]
+    save_workload("canonical_mixed_ref.npz", wl2, *run_ref(ref, hs, wl2, handles_b=hb))
+
+
 def main():
     build(ref=True)
     ref = Ref()
+    if sys.argv[1:] == ["canonical"]:
+        canonical_fixtures(ref)
+        return
 
     # 1. config-1 mesh (3,200-triangle (2,3) knots), 96 queries of the config-1 family, default seeds
     wl = workloads.config1(n=96, seed=101, device="cpu")
@@ -232,6 +269,7 @@ def main():
     geometry_vectors(ref)
     motion_vectors(ref)
     bvh_hashes(ref)
+    canonical_fixtures(ref)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,145 @@
+"""CANONICAL mode: every rotation step is seeded with the closest triangle
+pair found by the reference's distance query (C2A_Distance with rel_err =
+abs_err = 0), so the step no longer depends on traversal order.
+
+The oracle port's canonical mode is pinned against that composition of the
+reference's own functions (golden fixtures from tests/golden/make_golden.py,
+and the live reference where it is compiled); the warp-per-query CUDA kernel
+is checked against the port bit for bit.  Seeds are compared only for their
+distance: among exactly tied closest pairs the reference keeps the first one
+its depth-first search meets and the kernel the smallest pair.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from c2a_testutil import RESULT_FIELDS, bits, describe, load_fixture, result_mismatches
+
+FIELDS = [f for f in RESULT_FIELDS if f not in ("seed_a", "seed_b")]
+
+
+def canonical(params):
+    p = dict(params)
+    p["mode"] = 1
+    return p
+
+
+@pytest.mark.parametrize("name", ["canonical_config1", "canonical_mixed"])
+def test_port_canonical_matches_reference_fixture(port, name):
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    res, con = port.solve_batch(port.models(ms), qint, poses, canonical(params), threads=4,
+                                contacts_per_query=4096)
+    bad = result_mismatches(res, exp, con, econ, off)
+    assert not bad, f"{len(bad)} of {len(exp)} differ; first " + describe(res, exp, bad[0])
+
+
+def test_port_canonical_matches_live_reference(port):
+    from oracle.oracle import Ref
+    from c2a_gb300 import workloads
+
+    if not Ref.available():
+        pytest.skip("reference library not compiled here")
+    ref = Ref()
+    wl = workloads.small_knots(24, seed=31)
+    prm = canonical(wl.params)
+    ha, hb = ref.model(wl.meshes[0]), ref.model(wl.meshes[0])
+    res, con = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, prm, threads=4, contacts_per_query=1024)
+    for q in range(wl.n):
+        r, c = ref.solve(ha, hb, wl.poses[q], int(wl.qint[q, 2]), int(wl.qint[q, 3]), prm, max_contacts=1024)
+        assert all(bits(res[q][f]) == bits(r[f]) for f in RESULT_FIELDS), q
+        n = len(c)
+        assert bits(con[q][:n]["tri_a"]) == bits(c["tri_a"]) and bits(con[q][:n]["distance"]) == bits(c["distance"])
+
+
+def test_port_canonical_is_seed_independent(port):
+    """The first step's distance query finds the same minimum from any seed,
+    so every field but the reported seed pair is the same."""
+    from c2a_gb300 import workloads
+
+    wl = workloads.small_knots(32, seed=32)
+    prm = canonical(wl.params)
+    models = port.models(wl.meshes)
+    a, _ = port.solve_batch(models, wl.qint, wl.poses, prm, threads=4)
+    q2 = wl.qint.copy()
+    rng = np.random.default_rng(5)
+    q2[:, 2] = rng.integers(0, wl.meshes[0].num_tris, wl.n)
+    q2[:, 3] = rng.integers(0, wl.meshes[0].num_tris, wl.n)
+    b, _ = port.solve_batch(models, q2, wl.poses, prm, threads=4)
+    for f in FIELDS:
+        assert bits(a[f]) == bits(b[f]), f
+
+
+def _gpu(ctx, ms, qint, poses, params, slots):
+    ids = ctx.models(ms)
+    q = qint.copy()
+    q[:, 0] = np.asarray(ids)[qint[:, 0]]
+    q[:, 1] = np.asarray(ids)[qint[:, 1]]
+    return ctx.solve(q, poses, params, contacts_per_query=slots)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["canonical_config1", "canonical_mixed"])
+def test_gpu_canonical_matches_reference_fixture(gpu_ctx, name):
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    res, con = _gpu(gpu_ctx, ms, qint, poses, canonical(params), 4096)
+    assert (res["status"] == 0).all()
+    bad = result_mismatches(res, exp, con, econ, off, fields=FIELDS)
+    assert not bad, f"{len(bad)} of {len(exp)} differ; first " + describe(res, exp, bad[0], FIELDS)
+
+
+@pytest.mark.gpu
+def test_gpu_canonical_matches_port_config1(gpu_ctx, port):
+    from c2a_gb300 import workloads
+
+    wl = workloads.config1(n=1000, seed=1).subset(np.arange(400))
+    prm = canonical(wl.params)
+    res, con = _gpu(gpu_ctx, wl.meshes, wl.qint, wl.poses, prm, 512)
+    pres, pcon = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, prm, threads=os.cpu_count(),
+                                  contacts_per_query=512)
+    flat = np.concatenate([pcon[q][:min(512, pres[q]["num_contact"])] for q in range(wl.n)])
+    offs = np.concatenate([[0], np.cumsum(np.minimum(512, pres["num_contact"]))])
+    bad = result_mismatches(res, pres, con, flat, offs, fields=FIELDS)
+    assert not bad, describe(res, pres, bad[0], FIELDS)
+
+
+@pytest.mark.gpu
+def test_gpu_canonical_matches_port_mesh_families(gpu_ctx, port):
+    from c2a_gb300 import meshes, workloads
+
+    ms = [meshes.icosphere(3, radius=1.0, noise=0.02, seed=1), meshes.triangle_soup(1500, seed=2),
+          meshes.torus_knot(3, 5, 80, 10)]
+    rng = np.random.default_rng(14)
+    qi, ps = [], []
+    for k, (a, b) in enumerate([(0, 1), (1, 2), (2, 0), (1, 1)]):
+        q, p = workloads.ccd_queries(ms[a], ms[b], 30, 150 + k, gap_range=(0.0, 0.5), device="cpu", model_a=a,
+                                     model_b=b)
+        q[:, 2] = rng.integers(0, ms[a].num_tris, len(q))
+        q[:, 3] = rng.integers(0, ms[b].num_tris, len(q))
+        qi.append(q)
+        ps.append(p)
+    qint, poses = np.concatenate(qi), np.concatenate(ps)
+    prm = canonical(workloads.default_params(ms[0].bbox_diag(), 1e-3, 40))
+    res, con = _gpu(gpu_ctx, ms, qint, poses, prm, 256)
+    pres, pcon = port.solve_batch(port.models(ms), qint, poses, prm, threads=os.cpu_count(),
+                                  contacts_per_query=256)
+    flat = np.concatenate([pcon[q][:min(256, pres[q]["num_contact"])] for q in range(len(qint))])
+    offs = np.concatenate([[0], np.cumsum(np.minimum(256, pres["num_contact"]))])
+    bad = result_mismatches(res, pres, con, flat, offs, fields=FIELDS)
+    assert not bad, describe(res, pres, bad[0], FIELDS)
+
+
+@pytest.mark.gpu
+def test_gpu_canonical_config2_sample(gpu_ctx, port):
+    """64 queries of the 40,000-triangle config-2 workload."""
+    from c2a_gb300 import workloads
+
+    wl = workloads.config2(n=65536, seed=2, subset=64)
+    prm = canonical(wl.params)
+    res, con = _gpu(gpu_ctx, wl.meshes, wl.qint, wl.poses, prm, 256)
+    pres, pcon = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, prm, threads=os.cpu_count(),
+                                  contacts_per_query=256)
+    flat = np.concatenate([pcon[q][:min(256, pres[q]["num_contact"])] for q in range(wl.n)])
+    offs = np.concatenate([[0], np.cumsum(np.minimum(256, pres["num_contact"]))])
+    bad = result_mismatches(res, pres, con, flat, offs, fields=FIELDS)
+    assert not bad, describe(res, pres, bad[0], FIELDS)
