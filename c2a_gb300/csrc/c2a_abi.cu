@@ -15,6 +15,7 @@
 #include "../../include/c2a_gb300.h"
 #include "device/ca_front.cuh"
 #include "host/bvh_build.h"
+#include "wave_engine.h"
 
 using namespace c2a;
 
@@ -77,6 +78,7 @@ struct c2a_context {
     /* per-warp front slices of the canonical kernel (C2A_FRONT_CAP entries each) */
     Pending *d_fronts = nullptr;
     size_t fronts_warps = 0;
+    WaveBuffers *wave = nullptr; /* the batched canonical engine's lists */
     int canonical_blocks_per_sm = 0;
     std::mutex mu;
 };
@@ -136,7 +138,8 @@ c2a_status ensure_buf(c2a_context *ctx, size_t bytes)
 bool params_ok(const c2a_params *p)
 {
     return p && p->max_iters >= 0 && p->contacts_per_query >= 0 &&
-           (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL);
+           (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL) && p->engine >= C2A_ENGINE_AUTO &&
+           p->engine <= C2A_ENGINE_BATCHED;
 }
 
 /* queries must not pair models deeper than the traversal stack */
@@ -463,6 +466,7 @@ c2a_status c2a_destroy(c2a_context *ctx)
     for (ModelSlot &s : ctx->models) free_slot(s);
     if (ctx->d_models) cudaFree(ctx->d_models);
     if (ctx->d_fronts) cudaFree(ctx->d_fronts);
+    wave_free(ctx->wave);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_buf) cudaFree(ctx->d_buf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -595,6 +599,9 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     c2a_params prm = *params;
     if (!d_contacts) prm.contacts_per_query = 0;
+    if (prm.mode == C2A_MODE_CANONICAL && prm.engine == C2A_ENGINE_BATCHED)
+        return wave_solve(&ctx->wave, ctx->sm_count, s, d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
+                          d_results, d_contacts, &ctx->launches);
     if (prm.mode == C2A_MODE_CANONICAL) {
         if (!ctx->canonical_blocks_per_sm) {
             int occ = 0;

@@ -228,7 +228,8 @@ C2A_KDEV void warp_distance(Query &q, const M3 &Rroot, V3 Troot, Pending *stack,
             const int fc1 = __ldg(&q.A->nodes[e.b1].first_child), fc2 = __ldg(&q.B->nodes[e.b2].first_child);
             if (fc1 < 0 && fc2 < 0) {
                 const int ia = -fc1 - 1, ib = -fc2 - 1;
-                if ((double)tri_lower(q, ia, ib) <= best + margin) {
+                const float tl = tri_lower(q, ia, ib), ll = tl > e.d.v ? tl : e.d.v; /* or the leaf RSS bound */
+                if ((double)ll <= best + margin) {
                     C2A_STAT(q, ST_D_LEAF_EXACT);
                     V3 p, qq;
                     TriFeat f;

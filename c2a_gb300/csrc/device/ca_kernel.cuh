@@ -32,7 +32,7 @@ namespace c2a {
 
 /* the traversal is device code only (the geometry it calls is host+device) */
 #define C2A_KDEV __device__ __forceinline__
-#define C2A_KNOINL __device__ __noinline__
+#define C2A_KNOINL static __device__ __noinline__
 
 /* traversal stack depth; models are checked at upload: 2 * depth + 2 <= this */
 #ifndef C2A_STACK_DEPTH
@@ -47,7 +47,7 @@ enum {
     ST_D_ROUNDS, ST_D_POPS, ST_D_LEAF_EXACT, ST_D_KCYC, ST_T_ROUNDS, ST_T_POPS, ST_T_KCYC, ST_C_KCYC, ST_Q_KCYC,
     ST_COUNT
 };
-__device__ unsigned long long g_c2a_stats[ST_COUNT];
+static __device__ unsigned long long g_c2a_stats[ST_COUNT];
 #define C2A_STAT(q, i) ((q).st[i]++)
 #else
 #define C2A_STAT(q, i) ((void)0)

@@ -19,10 +19,14 @@ from c2a_testutil import RESULT_FIELDS, bits, describe, load_fixture, result_mis
 FIELDS = [f for f in RESULT_FIELDS if f not in ("seed_a", "seed_b")]
 
 
-def canonical(params):
+def canonical(params, engine=0):
     p = dict(params)
     p["mode"] = 1
+    p["engine"] = engine
     return p
+
+
+ENGINES = [1, 2]  # one warp per query; the batched wavefront engine
 
 
 @pytest.mark.parametrize("name", ["canonical_config1", "canonical_mixed"])
@@ -52,6 +56,21 @@ def test_port_canonical_matches_live_reference(port):
         assert bits(con[q][:n]["tri_a"]) == bits(c["tri_a"]) and bits(con[q][:n]["distance"]) == bits(c["distance"])
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", ENGINES)
+def test_gpu_canonical_translation(gpu_ctx, port, engine):
+    """Translation-only queries take the reference's sequential path (no
+    closest-pair seeding), contacts sorted by triangle pair."""
+    ms, qint, poses, params, exp, econ, off = load_fixture("translation")
+    prm = canonical(params, engine)
+    res, con = _gpu(gpu_ctx, ms, qint, poses, prm, 4096)
+    pres, pcon = port.solve_batch(port.models(ms), qint, poses, prm, threads=4, contacts_per_query=4096)
+    flat = np.concatenate([pcon[q][:min(4096, pres[q]["num_contact"])] for q in range(len(qint))])
+    offs = np.concatenate([[0], np.cumsum(np.minimum(4096, pres["num_contact"]))])
+    bad = result_mismatches(res, pres, con, flat, offs)
+    assert not bad, describe(res, pres, bad[0])
+
+
 def test_port_canonical_is_seed_independent(port):
     """The first step's distance query finds the same minimum from any seed,
     so every field but the reported seed pair is the same."""
@@ -79,21 +98,23 @@ def _gpu(ctx, ms, qint, poses, params, slots):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("name", ["canonical_config1", "canonical_mixed"])
-def test_gpu_canonical_matches_reference_fixture(gpu_ctx, name):
+def test_gpu_canonical_matches_reference_fixture(gpu_ctx, name, engine):
     ms, qint, poses, params, exp, econ, off = load_fixture(name)
-    res, con = _gpu(gpu_ctx, ms, qint, poses, canonical(params), 4096)
+    res, con = _gpu(gpu_ctx, ms, qint, poses, canonical(params, engine), 4096)
     assert (res["status"] == 0).all()
     bad = result_mismatches(res, exp, con, econ, off, fields=FIELDS)
     assert not bad, f"{len(bad)} of {len(exp)} differ; first " + describe(res, exp, bad[0], FIELDS)
 
 
 @pytest.mark.gpu
-def test_gpu_canonical_matches_port_config1(gpu_ctx, port):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_gpu_canonical_matches_port_config1(gpu_ctx, port, engine):
     from c2a_gb300 import workloads
 
     wl = workloads.config1(n=1000, seed=1).subset(np.arange(400))
-    prm = canonical(wl.params)
+    prm = canonical(wl.params, engine)
     res, con = _gpu(gpu_ctx, wl.meshes, wl.qint, wl.poses, prm, 512)
     pres, pcon = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, prm, threads=os.cpu_count(),
                                   contacts_per_query=512)
@@ -104,7 +125,8 @@ def test_gpu_canonical_matches_port_config1(gpu_ctx, port):
 
 
 @pytest.mark.gpu
-def test_gpu_canonical_matches_port_mesh_families(gpu_ctx, port):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_gpu_canonical_matches_port_mesh_families(gpu_ctx, port, engine):
     from c2a_gb300 import meshes, workloads
 
     ms = [meshes.icosphere(3, radius=1.0, noise=0.02, seed=1), meshes.triangle_soup(1500, seed=2),
@@ -119,7 +141,7 @@ def test_gpu_canonical_matches_port_mesh_families(gpu_ctx, port):
         qi.append(q)
         ps.append(p)
     qint, poses = np.concatenate(qi), np.concatenate(ps)
-    prm = canonical(workloads.default_params(ms[0].bbox_diag(), 1e-3, 40))
+    prm = canonical(workloads.default_params(ms[0].bbox_diag(), 1e-3, 40), engine)
     res, con = _gpu(gpu_ctx, ms, qint, poses, prm, 256)
     pres, pcon = port.solve_batch(port.models(ms), qint, poses, prm, threads=os.cpu_count(),
                                   contacts_per_query=256)
@@ -130,12 +152,13 @@ def test_gpu_canonical_matches_port_mesh_families(gpu_ctx, port):
 
 
 @pytest.mark.gpu
-def test_gpu_canonical_config2_sample(gpu_ctx, port):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_gpu_canonical_config2_sample(gpu_ctx, port, engine):
     """64 queries of the 40,000-triangle config-2 workload."""
     from c2a_gb300 import workloads
 
     wl = workloads.config2(n=65536, seed=2, subset=64)
-    prm = canonical(wl.params)
+    prm = canonical(wl.params, engine)
     res, con = _gpu(gpu_ctx, wl.meshes, wl.qint, wl.poses, prm, 256)
     pres, pcon = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, prm, threads=os.cpu_count(),
                                   contacts_per_query=256)
