@@ -47,7 +47,7 @@ class Params(C.Structure):
 
 
 MODE_REFERENCE, MODE_CANONICAL = 0, 1
-ENGINE_AUTO, ENGINE_WARP, ENGINE_BATCHED = 0, 1, 2
+ENGINE_AUTO, ENGINE_WARP, ENGINE_BATCHED, ENGINE_THREAD = 0, 1, 2, 3
 
 
 class Contacts:

@@ -14,6 +14,7 @@
 
 #include "../../include/c2a_gb300.h"
 #include "device/ca_front.cuh"
+#include "device/ca_warp.cuh"
 #include "host/bvh_build.h"
 #include "wave_engine.h"
 
@@ -80,6 +81,7 @@ struct c2a_context {
     size_t fronts_warps = 0;
     WaveBuffers *wave = nullptr; /* the batched canonical engine's lists */
     int canonical_blocks_per_sm = 0;
+    int warp_blocks_per_sm = 0;
     std::mutex mu;
 };
 
@@ -139,7 +141,8 @@ bool params_ok(const c2a_params *p)
 {
     return p && p->max_iters >= 0 && p->contacts_per_query >= 0 &&
            (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL) && p->engine >= C2A_ENGINE_AUTO &&
-           p->engine <= C2A_ENGINE_BATCHED;
+           p->engine <= C2A_ENGINE_THREAD && !(p->mode == C2A_MODE_REFERENCE && p->engine == C2A_ENGINE_BATCHED) &&
+           !(p->mode == C2A_MODE_CANONICAL && p->engine == C2A_ENGINE_THREAD);
 }
 
 /* queries must not pair models deeper than the traversal stack */
@@ -290,6 +293,29 @@ __global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *
     out.num_contact = cnt;
     out.contact_offset = qi * slots;
     out.status = q.status | (cnt > slots ? C2A_QUERY_CONTACT_OVERFLOW : 0);
+}
+
+/* REFERENCE mode on one warp per query (persistent): the reference's order,
+ * each node-pair test split across the lanes */
+__global__ void __launch_bounds__(kThreads) c2a_solve_warp_kernel(const c2a_query *__restrict__ queries, int n,
+                                                                  const DevModel *__restrict__ models,
+                                                                  int num_models, c2a_params prm,
+                                                                  c2a_result *__restrict__ results,
+                                                                  c2a_contact *__restrict__ contacts,
+                                                                  unsigned int *__restrict__ counter)
+{
+    __shared__ WarpShared sh[kThreads / 32];
+    Pending tstack[C2A_STACK_DEPTH]; /* the translation-only step's sequential stack */
+    const int lane = threadIdx.x & 31;
+    WarpShared &mine = sh[threadIdx.x >> 5];
+    for (;;) {
+        unsigned int q = 0;
+        if (lane == 0) q = atomicAdd(counter, 1u);
+        q = __shfl_sync(kFullMask, q, 0);
+        if (q >= (unsigned int)n) break;
+        c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
+        solve_query_warp(queries[q], models, num_models, prm, results[q], cq, mine, tstack, (int)q, lane);
+    }
 }
 
 /* CANONICAL mode: one warp per query (persistent; warps take queries from
@@ -630,6 +656,20 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
         return C2A_OK;
     }
     C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
+    if (prm.engine != C2A_ENGINE_THREAD) {
+        if (!ctx->warp_blocks_per_sm) {
+            int occ = 0;
+            C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_solve_warp_kernel, kThreads, 0));
+            ctx->warp_blocks_per_sm = occ > 0 ? occ : 1;
+        }
+        const int most = ctx->sm_count * ctx->warp_blocks_per_sm;
+        const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
+        c2a_solve_warp_kernel<<<need < most ? need : most, kThreads, 0, s>>>(
+            d_queries, n, ctx->d_models, (int)ctx->models.size(), prm, d_results, d_contacts, ctx->d_counter);
+        ctx->launches++;
+        C2A_CUDA(cudaGetLastError());
+        return C2A_OK;
+    }
     const Shape sh = shape_for(ctx, n);
     c2a_solve_kernel<<<sh.blocks, sh.threads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
                                                        d_results, d_contacts, ctx->d_counter);

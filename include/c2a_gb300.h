@@ -80,7 +80,7 @@ typedef struct c2a_params {
     int32_t qsize;              /* front capacity hint; never changes a result */
     int32_t contacts_per_query; /* contact slots per query in the output buffer */
     int32_t mode;               /* C2A_MODE_REFERENCE or C2A_MODE_CANONICAL */
-    int32_t engine;             /* CANONICAL only: C2A_ENGINE_*; never changes a result */
+    int32_t engine;             /* C2A_ENGINE_*; never changes a result */
 } c2a_params;
 
 /* C2A_MODE_REFERENCE: the reference's results bit for bit (its depth-first
@@ -95,16 +95,20 @@ typedef struct c2a_params {
 #define C2A_MODE_REFERENCE 0
 #define C2A_MODE_CANONICAL 1
 
-/* How CANONICAL batches run (results are identical):
- * C2A_ENGINE_AUTO     one warp per query (the faster engine on the workloads measured);
- * C2A_ENGINE_WARP     one warp per query, the query's node pairs in a warp-shared front
- *                     (asynchronous on the stream);
- * C2A_ENGINE_BATCHED  every query in lockstep CA iterations, each phase a series of
- *                     waves over all queries' node pairs (the call synchronises the
- *                     stream between waves). */
+/* How a batch runs (never changes a result):
+ * C2A_ENGINE_AUTO     one warp per query;
+ * C2A_ENGINE_WARP     one warp per query: REFERENCE mode keeps the reference's
+ *                     depth-first order and splits each node-pair test across the lanes
+ *                     (the sixteen RectDist cases, the nine TriDist segment pairs);
+ *                     CANONICAL mode walks a warp-shared front of node pairs;
+ * C2A_ENGINE_BATCHED  CANONICAL only: every query in lockstep CA iterations, each phase
+ *                     a series of waves over all queries' node pairs (the call
+ *                     synchronises the stream between waves);
+ * C2A_ENGINE_THREAD   REFERENCE only: one thread per query. */
 #define C2A_ENGINE_AUTO 0
 #define C2A_ENGINE_WARP 1
 #define C2A_ENGINE_BATCHED 2
+#define C2A_ENGINE_THREAD 3
 
 typedef struct c2a_result {
     int32_t collisionfree;

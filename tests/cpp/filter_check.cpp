@@ -13,6 +13,7 @@
 #include <cstring>
 
 #include "../../c2a_gb300/csrc/device/geom.cuh"
+#include "../../c2a_gb300/csrc/device/rect_cases.cuh"
 
 using namespace c2a;
 
@@ -199,6 +200,41 @@ int c2a_fc_tri(const double *ta, const double *tb, const double *Rm, const doubl
     out[6] = f.type_b;
     out[7] = fe.type_a;
     out[8] = fe.type_b;
+    return 0;
+}
+
+/*
+ * C2ARectDist two ways in FP64: the sequential rect_dist and the lane-parallel
+ * case form (cases 0..15 evaluated independently, the first that holds wins,
+ * else the face-separation tail).  out: d_seq, S_seq[3], d_lanes, S_lanes[3],
+ * winning case (-1: tail).
+ */
+int c2a_fc_rect_lanes(const double *Rab9, const double *Tab3, const double *a, const double *b, double *out)
+{
+    const M3 R = m3_of(Rab9);
+    const V3 T = v3(Tab3[0], Tab3[1], Tab3[2]);
+    ExactCtx xc{false};
+    V3 S = v3(0, 0, 0);
+    out[0] = rect_dist(R, T, a, b, S, xc);
+    out[1] = S.x; out[2] = S.y; out[3] = S.z;
+    int win = -1;
+    double d = 0.0;
+    V3 Sw = v3(0, 0, 0);
+    for (int j = 0; j < 16; j++) {
+        V3 Sj;
+        bool hit = false;
+        const double dj = rect_case(j, R, T, a, b, Sj, hit, xc);
+        if (hit) {
+            win = j;
+            d = dj;
+            Sw = Sj;
+            break;
+        }
+    }
+    if (win < 0) d = rect_tail(R, T, a, b, Sw, xc);
+    out[4] = d;
+    out[5] = Sw.x; out[6] = Sw.y; out[7] = Sw.z;
+    out[8] = win;
     return 0;
 }
 

@@ -249,3 +249,17 @@ def test_cpp_dropin_api(lib, port):
             toc, numca, ncont, cf = r[0], int(r[1]), int(r[2]), int(r[3])
             assert toc == pres[i]["toc"] and numca == pres[i]["numCA"], i
             assert cf == pres[i]["collisionfree"] and ncont == pres[i]["num_contact"], i
+
+
+@pytest.mark.parametrize("engine", [1, 3])
+@pytest.mark.parametrize("name", ["config1", "mixed"])
+def test_gpu_reference_engines_match_fixture(gpu_ctx, name, engine):
+    """Both reference-order kernels: one warp per query (the node-pair tests
+    split across the lanes) and one thread per query."""
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    prm = dict(params)
+    prm["engine"] = engine
+    res, con = gpu_solve(gpu_ctx, ms, qint, poses, prm)
+    assert (res["status"] == 0).all()
+    bad = result_mismatches(res, exp, con, econ, off)
+    assert not bad, f"engine {engine}: {len(bad)} of {len(exp)} differ; first " + describe(res, exp, bad[0])
