@@ -54,6 +54,9 @@ def parse():
     p.add_argument("--queries", type=int, default=65536)
     p.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU-baseline sample (0: auto)")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--mode", choices=["reference", "canonical"], default="reference",
+                   help="reference: the reference's results bit for bit; canonical: closest-pair-seeded steps")
+    p.add_argument("--engine", choices=["auto", "warp", "thread", "batched"], default="auto")
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
 
@@ -184,12 +187,22 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+ENGINES = {"auto": 0, "warp": 1, "batched": 2, "thread": 3}
+KERNELS = {("reference", "auto"): "c2a_solve_warp_kernel", ("reference", "warp"): "c2a_solve_warp_kernel",
+           ("reference", "thread"): "c2a_solve_kernel", ("canonical", "auto"): "c2a_canonical_kernel",
+           ("canonical", "warp"): "c2a_canonical_kernel", ("canonical", "batched"): "k_dsearch"}
+
+
 def config_dict(wl, args, sample_only=None):
+    traversal = ("reference order (FP64, bit-identical to the reference); one warp per query, each node-pair "
+                 "test split across the lanes" if args.mode == "reference" else
+                 "canonical: each step seeded with the exact closest pair (the reference's C2A_Distance), "
+                 "order-free front traversal; bit-identical to that composition of the reference's functions")
     return {"workload": wl.name, "queries": wl.n if sample_only is None else int(sample_only),
             "triangles_per_model": wl.meshes[0].num_tris, "models": "two (2,3) torus-knot tubes, 400 x 50",
             "th_ca": wl.params["th_ca"], "t_delta": wl.params["tol_t"], "qsize": wl.params["qsize"],
-            "traversal": "reference order (FP64, bit-identical to the reference)",
-            "seeding": "plain (triangle 0 of each model, as after EndModel)",
+            "mode": args.mode, "engine": args.engine, "traversal": traversal,
+            "seeding": "plain (triangle 0 of each model, as after EndModel); no learned seeding (not built)",
             "contacts_per_query": CONTACT_SLOTS, "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -218,6 +231,8 @@ def main():
     if dist:
         dist.barrier()
     wl = workloads.config2(n=args.queries, seed=2 + rank, device=f"cuda:{local}")
+    wl.params["mode"] = 1 if args.mode == "canonical" else 0
+    wl.params["engine"] = ENGINES[args.engine]
     ctx = api.Context(local)
     mid = ctx.model(wl.meshes[0])
     qint = wl.qint.copy()
@@ -283,10 +298,13 @@ def main():
     if prof and prof.get("dram_bytes_per_query"):
         traffic = float(prof["dram_bytes_per_query"]) * n
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_src, "kernel": "c2a_solve_kernel",
+                "traffic": traffic, "peak_source": peak_src, "kernel": KERNELS.get((args.mode, args.engine)),
                 "algorithmic_bytes_per_launch": alg_bytes, "num_bv_tests": bv, "num_tri_tests": tri,
-                "note": "the kernel is FP64-instruction bound (GB300 FP64 ~1/64 of FP32); node bytes are "
-                        "the reference's algorithmic reads, mostly served by L2"}
+                "note": "not HBM-bound: the traversal is a dependent chain of FP64 node-pair tests; its binding "
+                        "resource is the FP64 pipe (see fp64_pipe) and, for the heaviest queries, latency"}
+    if prof and prof.get("fp64_pipe_active_pct") is not None:
+        roofline["fp64_pipe"] = {"active_pct_of_peak": prof["fp64_pipe_active_pct"],
+                                 "source": prof.get("source", "profiles")}
 
     e2e = None
     if not args.no_e2e:

@@ -80,6 +80,8 @@ struct c2a_context {
     Pending *d_fronts = nullptr;
     size_t fronts_warps = 0;
     WaveBuffers *wave = nullptr; /* the batched canonical engine's lists */
+    int32_t *d_order = nullptr;  /* the order the warp kernel takes queries in */
+    size_t order_cap = 0;
     int canonical_blocks_per_sm = 0;
     int warp_blocks_per_sm = 0;
     std::mutex mu;
@@ -295,16 +297,57 @@ __global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *
     out.status = q.status | (cnt > slots ? C2A_QUERY_CONTACT_OVERFLOW : 0);
 }
 
+/* The order warps take queries in: queries whose bounding spheres close in on
+ * each other over the motion go first (they run many CA iterations), the
+ * rest after, so the longest queries do not start last.  Results are written
+ * by query index; the order changes nothing else. */
+__global__ void c2a_schedule_kernel(const c2a_query *__restrict__ queries, int n,
+                                    const DevModel *__restrict__ models, int num_models,
+                                    int32_t *__restrict__ order, unsigned int *__restrict__ ends)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const c2a_query &q = queries[i];
+    bool early = false;
+    if (q.model_a >= 0 && q.model_a < num_models && q.model_b >= 0 && q.model_b < num_models &&
+        (models[q.model_a].flags & C2A_MODEL_LIVE) && (models[q.model_b].flags & C2A_MODEL_LIVE)) {
+        const NodeRec *ra = models[q.model_a].nodes, *rb = models[q.model_b].nodes;
+        /* root rectangle centres and bounding radii in each model's frame */
+        const V3 ca = mul(load_R(ra), v3(0.5 * ra->l[0], 0.5 * ra->l[1], 0.0)) + load_Tr(ra);
+        const V3 cb = mul(load_R(rb), v3(0.5 * rb->l[0], 0.5 * rb->l[1], 0.0)) + load_Tr(rb);
+        const double rad = 0.5 * (ra->size + rb->size);
+        const double *P = q.pose;
+        const V3 pa0 = mul(pose_R(P), ca) + pose_T(P), pb0 = mul(pose_R(P + 24), cb) + pose_T(P + 24);
+        const V3 pa1 = mul(pose_R(P + 12), ca) + pose_T(P + 12), pb1 = mul(pose_R(P + 36), cb) + pose_T(P + 36);
+        const V3 g0 = pb0 - pa0, g1 = pb1 - pa1;
+        /* the segment between the centres' relative start and end positions comes within reach */
+        const V3 dg = g1 - g0;
+        const double L2 = dot(dg, dg);
+        double t = L2 > 0 ? -dot(g0, dg) / L2 : 0.0;
+        t = t < 0 ? 0 : (t > 1 ? 1 : t);
+        const V3 gm = g0 + mul_s(dg, t);
+        early = dot(gm, gm) < rad * rad;
+    }
+    const unsigned int k = atomicAdd(ends + (early ? 0 : 1), 1u);
+    if (early) order[k] = i;
+    else order[n - 1 - (int)k] = i;
+}
+
 /* REFERENCE mode on one warp per query (persistent): the reference's order,
  * each node-pair test split across the lanes */
-__global__ void __launch_bounds__(kThreads) c2a_solve_warp_kernel(const c2a_query *__restrict__ queries, int n,
+#ifndef C2A_WARP_MINB
+#define C2A_WARP_MINB 1
+#endif
+__global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel(const c2a_query *__restrict__ queries, int n,
                                                                   const DevModel *__restrict__ models,
                                                                   int num_models, c2a_params prm,
                                                                   c2a_result *__restrict__ results,
                                                                   c2a_contact *__restrict__ contacts,
-                                                                  unsigned int *__restrict__ counter)
+                                                                  unsigned int *__restrict__ counter,
+                                                                  const int32_t *__restrict__ order)
 {
-    __shared__ WarpShared sh[kThreads / 32];
+    extern __shared__ unsigned char c2a_warp_smem[];
+    WarpShared *sh = reinterpret_cast<WarpShared *>(c2a_warp_smem);
     Pending tstack[C2A_STACK_DEPTH]; /* the translation-only step's sequential stack */
     const int lane = threadIdx.x & 31;
     WarpShared &mine = sh[threadIdx.x >> 5];
@@ -313,6 +356,7 @@ __global__ void __launch_bounds__(kThreads) c2a_solve_warp_kernel(const c2a_quer
         if (lane == 0) q = atomicAdd(counter, 1u);
         q = __shfl_sync(kFullMask, q, 0);
         if (q >= (unsigned int)n) break;
+        if (order) q = (unsigned int)order[q];
         c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
         solve_query_warp(queries[q], models, num_models, prm, results[q], cq, mine, tstack, (int)q, lane);
     }
@@ -492,6 +536,7 @@ c2a_status c2a_destroy(c2a_context *ctx)
     for (ModelSlot &s : ctx->models) free_slot(s);
     if (ctx->d_models) cudaFree(ctx->d_models);
     if (ctx->d_fronts) cudaFree(ctx->d_fronts);
+    if (ctx->d_order) cudaFree(ctx->d_order);
     wave_free(ctx->wave);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_buf) cudaFree(ctx->d_buf);
@@ -657,16 +702,31 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
     }
     C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
     if (prm.engine != C2A_ENGINE_THREAD) {
+        const size_t smem = sizeof(WarpShared) * (kThreads / 32);
         if (!ctx->warp_blocks_per_sm) {
+            C2A_CUDA(cudaFuncSetAttribute(c2a_solve_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
             int occ = 0;
-            C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_solve_warp_kernel, kThreads, 0));
+            C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_solve_warp_kernel, kThreads, smem));
             ctx->warp_blocks_per_sm = occ > 0 ? occ : 1;
         }
         const int most = ctx->sm_count * ctx->warp_blocks_per_sm;
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
-        c2a_solve_warp_kernel<<<need < most ? need : most, kThreads, 0, s>>>(
-            d_queries, n, ctx->d_models, (int)ctx->models.size(), prm, d_results, d_contacts, ctx->d_counter);
-        ctx->launches++;
+        if ((size_t)n > ctx->order_cap) {
+            C2A_CUDA(cudaStreamSynchronize(s));
+            if (ctx->d_order) cudaFree(ctx->d_order);
+            ctx->d_order = nullptr;
+            ctx->order_cap = 0;
+            C2A_CUDA(cudaMalloc(&ctx->d_order, sizeof(int32_t) * (size_t)n));
+            ctx->order_cap = (size_t)n;
+        }
+        C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 1, 0, 2 * sizeof(unsigned int), s));
+        c2a_schedule_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(),
+                                                             ctx->d_order, ctx->d_counter + 1);
+        c2a_solve_warp_kernel<<<need < most ? need : most, kThreads, smem, s>>>(
+            d_queries, n, ctx->d_models, (int)ctx->models.size(), prm, d_results, d_contacts, ctx->d_counter,
+            ctx->d_order);
+        ctx->launches += 2;
         C2A_CUDA(cudaGetLastError());
         return C2A_OK;
     }

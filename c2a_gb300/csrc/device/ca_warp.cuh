@@ -31,10 +31,19 @@ namespace c2a {
 
 constexpr unsigned kWFull = 0xffffffffu;
 
-/* a pending second child: the pair, its d and mint, its exact transform */
+/* 1: node-pair and leaf tests through the certified FP32 filter (FP64 only
+ * where it cannot decide); 0: every test in FP64 */
+#ifndef C2A_WARP_FILTER
+#define C2A_WARP_FILTER 0
+#endif
+
+/* a child pair: its d and mint as certified FP32 values (d_e, m_e) or, once
+ * exact, the reference's FP64 values (d, m); its exact transform */
 struct WStackEntry {
     int32_t b1, b2;
+    int32_t exact, pad;
     double d, m;
+    EF d_e, m_e;
     M3 R;
     V3 T;
 };
@@ -47,6 +56,9 @@ struct WarpShared {
 
 C2A_KDEV double shfl_d(double v, int src) { return __shfl_sync(kWFull, v, src); }
 C2A_KDEV V3 shfl_v3(V3 v, int src) { return v3(shfl_d(v.x, src), shfl_d(v.y, src), shfl_d(v.z, src)); }
+C2A_KDEV EF K_EF1() { return ef_exact(1.0f); }
+C2A_KDEV EF shfl_e(EF v, int src) { return EF{__shfl_sync(kWFull, v.v, src), __shfl_sync(kWFull, v.e, src)}; }
+C2A_KDEV V3T<EF> shfl_v3e(V3T<EF> v, int src) { return v3t(shfl_e(v.x, src), shfl_e(v.y, src), shfl_e(v.z, src)); }
 
 /* ------------------------------------------------------------- TriDist */
 
@@ -164,6 +176,117 @@ C2A_KDEV double tri_dist_warp(const V3 S[3], const V3 Tt[3], V3 &P, V3 &Q, TriFe
     return 0.0;
 }
 
+/* the FP32 filter of TriDist on the warp: the distance with a certified
+ * bound, or ok = false when a decision of the reference's TriDist cannot be
+ * certified (the caller then computes it in FP64) */
+C2A_KDEV EF tri_dist_warp_e(const V3T<EF> S[3], const V3T<EF> Tt[3], TriFeat &f, bool &ok, int lane)
+{
+    EFCtx ctx{false};
+    const EF zero = ef_exact(0.0f);
+    V3T<EF> Sv[3], Tv[3];
+    Sv[0] = S[1] - S[0];
+    Sv[1] = S[2] - S[1];
+    Sv[2] = S[0] - S[2];
+    Tv[0] = Tt[1] - Tt[0];
+    Tv[1] = Tt[2] - Tt[1];
+    Tv[2] = Tt[0] - Tt[2];
+    V3T<EF> VEC = v3t(zero, zero, zero), Pk = VEC, Qk = VEC;
+    EF dd = zero, ak = zero, bk = zero, pk = zero;
+    bool lbad = false;
+    if (lane < 9) {
+        EFCtx lc{false};
+        const int i = lane / 3, j = lane % 3;
+        seg_pair(VEC, Pk, Qk, S[i], Sv[i], Tt[j], Tv[j], lc);
+        const V3T<EF> V = Qk - Pk;
+        dd = dot(V, V);
+        ak = dot(S[(i + 2) % 3] - Pk, VEC);
+        bk = dot(Tt[(j + 2) % 3] - Qk, VEC);
+        pk = dot(V, VEC);
+        lbad = lc.bad;
+    }
+    EF tp = zero, nl = zero;
+    V3T<EF> n = v3t(zero, zero, zero);
+    bool disj = false;
+    int point = -1;
+    if (lane == 9 || lane == 10) {
+        EFCtx vc{false};
+        point = lane == 9 ? vertex_over_face(S, Sv, Tt, tp, nl, n, disj, vc) : vertex_over_face(Tt, Tv, S, tp, nl, n, disj, vc);
+        lbad = vc.bad;
+    }
+    __syncwarp();
+    const unsigned badm = __ballot_sync(kWFull, lbad);
+    EF mindd = dist2(S[0], Tt[0]) + K_EF1();
+    int mink = -1;
+    bool shown_disjoint = false;
+    for (int k = 0; k < 9; k++) {
+        const EF ddk = shfl_e(dd, k), ak_ = shfl_e(ak, k), bk_ = shfl_e(bk, k), pk_ = shfl_e(pk, k);
+        if ((badm >> k) & 1u) ctx.bad = true;
+        if (cmp_le(ddk, mindd, ctx, 0)) {
+            mindd = ddk;
+            mink = k;
+            if (cmp_le(ak_, zero, ctx, 0) && cmp_le(zero, bk_, ctx, 0)) {
+                f.type_a = 1;
+                f.fid_a = k / 3;
+                f.type_b = 1;
+                f.fid_b = k % 3;
+                ok = !ctx.bad;
+                return num_sqrt(ddk);
+            }
+            const EF a = max0_c(ak_), b = min0_c(bk_);
+            if (cmp_lt(zero, pk_ - a + b, ctx, 0)) shown_disjoint = true;
+        }
+    }
+    if ((badm >> 9) & 1u) ctx.bad = true;
+    const int p0 = __shfl_sync(kWFull, point, 9), p1 = __shfl_sync(kWFull, point, 10);
+    const bool d0 = __shfl_sync(kWFull, (int)disj, 9) != 0, d1 = __shfl_sync(kWFull, (int)disj, 10) != 0;
+    if (mink >= 0) {
+        f.type_a = 1;
+        f.fid_a = mink / 3;
+        f.type_b = 1;
+        f.fid_b = mink % 3;
+    }
+    shown_disjoint = shown_disjoint || d0;
+    if (p0 >= 0) {
+        EF dw = zero;
+        bool wb = false;
+        if (lane == 9) {
+            EFCtx wc{false};
+            const V3T<EF> Pw = add_mul(Tt[point], n, num_div(tp, nl, wc));
+            dw = num_sqrt(dist2(Pw, Tt[point]));
+            wb = wc.bad;
+        }
+        f.type_a = 2;
+        f.fid_a = -1;
+        f.type_b = 0;
+        f.fid_b = p0;
+        ok = !ctx.bad && !__shfl_sync(kWFull, (int)wb, 9);
+        return shfl_e(dw, 9);
+    }
+    if ((badm >> 10) & 1u) ctx.bad = true;
+    shown_disjoint = shown_disjoint || d1;
+    if (p1 >= 0) {
+        EF dw = zero;
+        bool wb = false;
+        if (lane == 10) {
+            EFCtx wc{false};
+            const V3T<EF> Qw = add_mul(S[point], n, num_div(tp, nl, wc));
+            dw = num_sqrt(dist2(S[point], Qw));
+            wb = wc.bad;
+        }
+        f.type_a = 0;
+        f.fid_a = p1;
+        f.type_b = 2;
+        f.fid_b = -1;
+        ok = !ctx.bad && !__shfl_sync(kWFull, (int)wb, 10);
+        return shfl_e(dw, 10);
+    }
+    ok = !ctx.bad;
+    if (shown_disjoint) return num_sqrt(mindd);
+    f.type_a = f.type_b = -1; /* collided: left to the FP64 path */
+    ok = false;
+    return zero;
+}
+
 /* TriDist of leaf pair (ia, ib): B's triangle placed by (Rm, Tm) */
 C2A_KDEV double tri_distance_warp(const Query &q, int ia, int ib, V3 &p, V3 &qq, TriFeat &f, bool &col, int lane)
 {
@@ -176,6 +299,18 @@ C2A_KDEV double tri_distance_warp(const Query &q, int ia, int ib, V3 &p, V3 &qq,
     return tri_dist_warp(S, T, p, qq, f, col, lane);
 }
 
+/* the FP32 filter of a leaf pair's TriDist (needs q.shadows_ok) */
+C2A_KDEV EF tri_distance_warp_e(const Query &q, int ia, int ib, TriFeat &f, bool &ok, int lane)
+{
+    V3T<EF> S[3], T[3], t[3];
+    load_tri_e(S, q.A->stris + ia);
+    load_tri_e(t, q.B->stris + ib);
+    T[0] = mul_add(q.Rme, t[0], q.Tme);
+    T[1] = mul_add(q.Rme, t[1], q.Tme);
+    T[2] = mul_add(q.Rme, t[2], q.Tme);
+    return tri_dist_warp_e(S, T, f, ok, lane);
+}
+
 /* ------------------------------------------------------- child pair tests */
 
 /* C2A_BV_Distance of this half-warp's child pair (x1, x2) placed by (R, T):
@@ -185,9 +320,10 @@ C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const doubl
     ExactCtx xc{false};
     const int half = lane >> 4, j = lane & 15;
     V3 Sj = v3(0, 0, 0);
-    bool hit = false;
-    const double dj = rect_case(j, R, T, a, b, Sj, hit, xc);
-    const unsigned m = (__ballot_sync(kWFull, hit) >> (16 * half)) & 0xffffu;
+    int hit = 0;
+    bool vbad = false;
+    const double dj = rect_case(j, R, T, a, b, Sj, hit, vbad, xc);
+    const unsigned m = (__ballot_sync(kWFull, hit == 1) >> (16 * half)) & 0xffffu;
     const int win = m ? __ffs(m) - 1 : 0;
     const int src = 16 * half + win;
     const double dw = shfl_d(dj, src);
@@ -202,14 +338,10 @@ C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const doubl
     return dt;
 }
 
-/* the two children of an expanded pair, tested like bv_test_x; each half
- * computes one child (transform, distance, motion bounds) and writes it to
- * sh.child[half]; nbv is counted by the caller */
-C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, const M3 &PR, V3 PT, WarpShared &sh,
-                          int lane)
+/* the children of an internal pair (C2A.cpp:1192-1226) */
+C2A_KDEV void split_pair(const Query &q, int b1, int b2, int fc1, int fc2, int &side, int &a1, int &a2, int &c1,
+                         int &c2)
 {
-    const int half = lane >> 4;
-    int side, a1, a2, c1, c2;
     if (fc2 < 0 || (fc1 >= 0 && (__ldg(&q.A->nodes[b1].size) > __ldg(&q.B->nodes[b2].size)))) {
         side = 0;
         a1 = fc1; c1 = fc1 + 1;
@@ -219,18 +351,19 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
         a1 = c1 = b1;
         a2 = fc2; c2 = fc2 + 1;
     }
-    const int x1 = half ? c1 : a1, x2 = half ? c2 : a2;
-    M3 R;
-    V3 T;
-    child_transform(q, side, x1, x2, PR, PT, R, T);
+}
+
+/* bv_test_x of child pair (x1, x2) placed by (R, T), exactly, on one half-warp */
+C2A_KDEV void child_test_x(const Query &q, int x1, int x2, const M3 &R, V3 T, double &d, double &mint, int lane)
+{
     NodeX n1, n2;
     load_x(n1, q.A->nodes + x1);
     load_x(n2, q.B->nodes + x2);
     V3 S = v3(0, 0, 0);
     double z = rect_dist_half(R, T, n1.l, n2.l, S, lane);
     z -= (n1.r + n2.r);
-    const double d = max0_c(z);
-    double mint = 0.0;
+    d = max0_c(z);
+    mint = 0.0;
     if (d != 0.0 && q.want_mint) {
         ExactCtx xc{false};
         V3 S1 = mul(q.r1, mul(n1.Rloc, S));
@@ -239,29 +372,166 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
         const double mb2 = bound_rss(q.x2, n2.angR, S2, xc);
         mint = max0_c((d) / (mb1 + mb2));
     }
+}
+
+/* the same with the FP32 filter; false when a half cannot certify it */
+C2A_KDEV bool child_test_e(const Query &q, int x1, int x2, const M3 &R, V3 T, EF &d, EF &mint, bool &d_zero,
+                           int lane)
+{
+    const int half = lane >> 4, j = lane & 15;
+    EFCtx pc{!q.shadows_ok};
+    const M3T<EF> Re = ef_m3(R, pc);
+    const V3T<EF> Te = ef_v3(T, pc);
+    NodeE n1, n2;
+    load_e(n1, q.A->snodes + x1);
+    load_e(n2, q.B->snodes + x2);
+    const EF zero = ef_exact(0.0f);
+    V3T<EF> Sj = v3t(zero, zero, zero);
+    int hit = 0;
+    bool vbad = false;
+    const EF dj = rect_case(j, Re, Te, n1.l, n2.l, Sj, hit, vbad, pc);
+    const unsigned nz = (__ballot_sync(kWFull, hit != 0) >> (16 * half)) & 0xffffu;
+    const int src = 16 * half + (nz ? __ffs(nz) - 1 : 0);
+    const int hw = __shfl_sync(kWFull, hit, src);
+    const bool vb = __shfl_sync(kWFull, (int)vbad, src) != 0;
+    const EF dw = shfl_e(dj, src);
+    const V3T<EF> Sw = shfl_v3e(Sj, src);
+    bool ok;
+    EF dist;
+    V3T<EF> S;
+    if (nz) {
+        ok = hw == 1 && !vb;
+        dist = dw;
+        S = Sw;
+    } else {
+        EFCtx tc{pc.bad};
+        V3T<EF> St = v3t(zero, zero, zero);
+        dist = rect_tail(Re, Te, n1.l, n2.l, St, tc);
+        S = St;
+        ok = !tc.bad;
+    }
+    const EF z = dist - (n1.r + n2.r);
+    const int pos = ef_lt3(zero, z);
+    if (pos < 0) ok = false;
+    d_zero = pos == 0;
+    d = d_zero ? zero : z;
+    mint = zero;
+    if (ok && !d_zero && q.want_mint) {
+        EFCtx bc{false};
+        V3T<EF> S1 = mul(q.r1e, mul(n1.Rloc, S));
+        V3T<EF> S2 = mul_s(S1, ef_exact(-1.0f));
+        const EF mb1 = bound_rss(q.e1, n1.angR, S1, bc);
+        const EF mb2 = bound_rss(q.e2, n2.angR, S2, bc);
+        mint = max0_c(ef_div(d, mb1 + mb2, bc));
+        ok = !bc.bad;
+    }
+    return ok;
+}
+
+/* the two children of an expanded pair into sh.child[0] (a) and sh.child[1]
+ * (c): each half tests one with the FP32 filter; if a half cannot certify
+ * its child, both are tested in FP64 */
+C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, const M3 &PR, V3 PT, WarpShared &sh,
+                          int lane)
+{
+    const int half = lane >> 4;
+    int side, a1, a2, c1, c2;
+    split_pair(q, b1, b2, fc1, fc2, side, a1, a2, c1, c2);
+    const int x1 = half ? c1 : a1, x2 = half ? c2 : a2;
+    M3 R;
+    V3 T;
+    child_transform(q, side, x1, x2, PR, PT, R, T);
+    EF d = ef_exact(0.0f), m = ef_exact(0.0f);
+    bool d_zero = false;
+    const bool ok = C2A_WARP_FILTER && child_test_e(q, x1, x2, R, T, d, m, d_zero, lane);
+    double dx = 0.0, mx = 0.0;
+    int exact = d_zero ? 1 : 0; /* d = max(z, 0) = 0 and mint = 0 exactly */
+    if (!__all_sync(kWFull, ok)) {
+        child_test_x(q, x1, x2, R, T, dx, mx, lane);
+        exact = 1;
+    }
     if ((lane & 15) == 0) {
         WStackEntry &e = sh.child[half];
         e.b1 = x1;
         e.b2 = x2;
-        e.d = d;
-        e.m = mint;
+        e.exact = exact;
+        e.pad = 0;
+        e.d = dx;
+        e.m = mx;
+        e.d_e = d;
+        e.m_e = m;
+        if (exact) { /* the FP32 views of exact values decide too */
+            EFCtx cc{false};
+            e.d_e = in_d(dx, cc);
+            e.m_e = in_d(mx, cc);
+            if (cc.bad) e.d_e = e.m_e = EF{0.0f, __int_as_float(0x7f800000)};
+        }
         e.R = R;
         e.T = T;
     }
     __syncwarp();
 }
 
+/* the exact d and mint of a child pair (both halves compute it; uniform) */
+C2A_KDEV void make_exact_warp(const Query &q, WStackEntry &e, int lane)
+{
+    if (e.exact) return;
+    child_test_x(q, e.b1, e.b2, e.R, e.T, e.d, e.m, lane);
+    EFCtx cc{false};
+    e.d_e = in_d(e.d, cc);
+    e.m_e = in_d(e.m, cc);
+    if (cc.bad) e.d_e = e.m_e = EF{0.0f, __int_as_float(0x7f800000)};
+    e.exact = 1;
+}
+
 /* ------------------------------------------------------------ the step */
 
-C2A_KDEV bool descend_w(const Query &q, double m, double d)
+/* mint < UpboundTOC && (d < distance - abs_err || d * (1 + rel_err) < distance) (C2A.cpp:1281-1351) */
+C2A_KDEV bool descend_w(const Query &q, WStackEntry &e, int lane)
 {
-    return m < q.upbound && ((d < (q.distance - q.abs_err)) || (d * (1 + q.rel_err) < q.distance));
+    if (q.shadows_ok) {
+        const int a = ef_lt3(e.m_e, q.upbound_e);
+        const int b = ef_lt3(e.d_e, q.bound_e);
+        const int c = ef_lt3(e.d_e * q.rel1_e, q.distance_e);
+        const int r = and3(a, or3(b, c));
+        if (r >= 0) return r == 1;
+    }
+    make_exact_warp(q, e, lane);
+    return e.m < q.upbound && ((e.d < (q.distance - q.abs_err)) || (e.d * (1 + q.rel_err) < q.distance));
+}
+
+/* a pruned pair's mint lowers res->mint (C2A.cpp:1290-1311) */
+C2A_KDEV void contribute_w(Query &q, WStackEntry &e, int lane)
+{
+    if (q.shadows_ok && ef_lt3(e.m_e, q.mint_e) == 0) return; /* certainly >= the current minimum */
+    make_exact_warp(q, e, lane);
+    if (e.m < q.mint) {
+        q.mint = e.m;
+        refresh_mint_shadow(q);
+    }
+}
+
+/* d2 < d1 (C2A.cpp:1281) */
+C2A_KDEV bool closer_second_w(const Query &q, WStackEntry &a, WStackEntry &c, int lane)
+{
+    const int r = ef_lt3(c.d_e, a.d_e);
+    if (r >= 0 && q.shadows_ok) return r == 1;
+    make_exact_warp(q, a, lane);
+    make_exact_warp(q, c, lane);
+    return c.d < a.d;
 }
 
 /* a leaf pair of the rotation step (C2A.cpp:1141-1183) */
 C2A_KDEV void leaf_step_warp(Query &q, int b1, int b2, int fc1, int fc2, int lane)
 {
     const int ia = -fc1 - 1, ib = -fc2 - 1;
+    q.ntri++;
+    if (C2A_WARP_FILTER && q.shadows_ok) { /* most leaves cannot reach the running distance */
+        TriFeat fe;
+        bool ok = false;
+        const EF de = tri_distance_warp_e(q, ia, ib, fe, ok, lane);
+        if (ok && ef_le3(de, q.distance_e) == 0) return;
+    }
     V3 p, qq;
     TriFeat f;
     bool col = false;
@@ -278,8 +548,8 @@ C2A_KDEV void leaf_step_warp(Query &q, int b1, int b2, int fc1, int fc2, int lan
         double mint = (dTri) / (mb1 + mb2);
         if (mint < 0.0) mint = 0.0;
         if (mint <= q.mint) q.mint = mint;
+        refresh_shadows(q);
     }
-    q.ntri++;
 }
 
 /* TOCStepRecurse_Dis from the root pair, in the reference's order */
@@ -301,32 +571,32 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
             }
             expand_warp(q, b1, b2, fc1, fc2, R, T, sh, lane);
             q.nbv += 2;
-            const WStackEntry &a = sh.child[0], &c = sh.child[1];
-            const bool c_first = c.d < a.d; /* d2 < d1 (C2A.cpp:1281) */
-            const WStackEntry &first = c_first ? c : a;
+            WStackEntry a = sh.child[0], c = sh.child[1];
+            const bool c_first = closer_second_w(q, a, c, lane);
+            WStackEntry &first = c_first ? c : a;
             if (lane == 0) sh.stack[sp] = c_first ? a : c;
             sp++;
-            if (descend_w(q, first.m, first.d)) {
+            if (descend_w(q, first, lane)) {
                 b1 = first.b1;
                 b2 = first.b2;
                 R = first.R;
                 T = first.T;
                 go = true;
-            } else if (first.m < q.mint) {
-                q.mint = first.m;
+            } else {
+                contribute_w(q, first, lane);
             }
             __syncwarp();
         }
         while (!go && sp > 0) {
-            const WStackEntry &e = sh.stack[--sp];
-            if (descend_w(q, e.m, e.d)) {
+            WStackEntry e = sh.stack[--sp];
+            if (descend_w(q, e, lane)) {
                 b1 = e.b1;
                 b2 = e.b2;
                 R = e.R;
                 T = e.T;
                 go = true;
-            } else if (e.m < q.mint) {
-                q.mint = e.m;
+            } else {
+                contribute_w(q, e, lane);
             }
         }
         __syncwarp();
@@ -355,6 +625,7 @@ C2A_KDEV void toc_step_warp(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, WarpShared
         q.rel_err = (q.numCA <= 2) ? 3 : 0.5;
     }
     q.mint = 1;
+    refresh_shadows(q);
     toc_dfs_warp(q, R, T, sh, lane);
 }
 
@@ -365,6 +636,14 @@ C2A_KDEV bool contact_leaf_warp(Query &q, int fc1, int fc2, double threshold, in
                                 int lane)
 {
     const int ia = -fc1 - 1, ib = -fc2 - 1;
+    if (C2A_WARP_FILTER && q.shadows_ok) {
+        EFCtx tc{false};
+        const EF threshold_e = in_d(threshold, tc);
+        TriFeat fe{-1, -1, -1, -1};
+        bool ok = false;
+        const EF de = tri_distance_warp_e(q, ia, ib, fe, ok, lane);
+        if (ok && !tc.bad && fe.type_a != -1 && fe.type_b != -1 && ef_le3(de, threshold_e) == 0) return false;
+    }
     V3 p, qq;
     TriFeat f{-1, -1, -1, -1};
     bool col = false;
@@ -391,6 +670,19 @@ C2A_KDEV bool contact_leaf_warp(Query &q, int fc1, int fc2, double threshold, in
     return true;
 }
 
+/* d < threshold (abs_err = rel_err = 0: both of the reference's clauses) */
+C2A_KDEV bool contact_descend_w(const Query &q, WStackEntry &e, double threshold, int lane)
+{
+    if (q.shadows_ok) {
+        EFCtx tc{false};
+        const EF te = in_d(threshold, tc);
+        const int r = tc.bad ? -1 : ef_lt3(e.d_e, te);
+        if (r >= 0) return r == 1;
+    }
+    make_exact_warp(q, e, lane);
+    return (e.d < (threshold - 0)) || (e.d * (1.0 + 0) < threshold);
+}
+
 /* TOCStepRecurse_Dis_contact with a fixed threshold (C2A.cpp:1525-1725):
  * contacts in visiting order; returns how many were found */
 C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double threshold, WarpShared &sh,
@@ -415,12 +707,12 @@ C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double thresh
                 return count;
             }
             expand_warp(q, b1, b2, fc1, fc2, R, T, sh, lane);
-            const WStackEntry &a = sh.child[0], &c = sh.child[1];
-            const bool c_first = c.d < a.d;
-            const WStackEntry &first = c_first ? c : a;
+            WStackEntry a = sh.child[0], c = sh.child[1];
+            const bool c_first = closer_second_w(q, a, c, lane);
+            WStackEntry &first = c_first ? c : a;
             if (lane == 0) sh.stack[sp] = c_first ? a : c;
             sp++;
-            if ((first.d < (threshold - 0)) || (first.d * (1.0 + 0) < threshold)) {
+            if (contact_descend_w(q, first, threshold, lane)) {
                 b1 = first.b1;
                 b2 = first.b2;
                 R = first.R;
@@ -430,8 +722,8 @@ C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double thresh
             __syncwarp();
         }
         while (!go && sp > 0) {
-            const WStackEntry &e = sh.stack[--sp];
-            if ((e.d < (threshold - 0)) || (e.d * (1.0 + 0) < threshold)) {
+            WStackEntry e = sh.stack[--sp];
+            if (contact_descend_w(q, e, threshold, lane)) {
                 b1 = e.b1;
                 b2 = e.b2;
                 R = e.R;
@@ -569,6 +861,7 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
             V3 T;
             set_pose1(q, Ra, Ta);
             relative_transforms(q, Ra, Ta, Rb, Tb, R, T);
+            q.shadows_ok = q.e_ok && ((q.A->flags & q.B->flags) & C2A_MODEL_SHADOW_OK);
             q.want_mint = false;
             const int n = contact_dfs_warp(q, R, T, threshold, sh, contacts, prm.contacts_per_query, query_index,
                                            lane);

@@ -144,11 +144,18 @@ def main():
     w("")
     w("namespace c2a {")
     w("")
-    w("/* case j (0..15) of C2ARectDist; hit: its condition holds (the caller takes")
-    w(" * the first such case); S: Q - P of its edge pair; returns the distance */")
+    w("/* Kleene AND / OR over {1, 0, -1 (undecided)} */")
+    w("C2A_DEV int rc_and3(int a, int b) { return (a == 0 || b == 0) ? 0 : (a == 1 && b == 1) ? 1 : -1; }")
+    w("C2A_DEV int rc_or3(int a, int b) { return (a == 1 || b == 1) ? 1 : (a == 0 && b == 0) ? 0 : -1; }")
+    w("")
+    w("/* case j (0..15) of C2ARectDist.  hit: 1 its condition holds, 0 it does not,")
+    w(" * -1 undecided (the FP32 filter only; each part keeps its own context, so a")
+    w(" * part the sequential form would not evaluate decides nothing); vbad: the")
+    w(" * distance and S are not certified; ctx: the shared preamble's decisions.")
+    w(" * The caller takes the first case that holds. */")
     w("template <class T, class C>")
-    w("C2A_DEV T rect_case(int j, const M3T<T> &Rab, V3T<T> Tab, const T a[2], const T b[2], V3T<T> &S, bool &hit,")
-    w("                    C &ctx)")
+    w("C2A_DEV T rect_case(int j, const M3T<T> &Rab, V3T<T> Tab, const T a[2], const T b[2], V3T<T> &S, int &hit,")
+    w("                    bool &vbad, C &ctx)")
     w("{")
     for line in pre.strip("\n").split("\n"):
         w(line)
@@ -170,13 +177,17 @@ def main():
     w("    default:")
     w("        break;")
     w("    }")
-    w("    /* every part evaluated on every lane: all are pure */")
-    w("    const bool k0 = LT(L[0], R[0]), k1 = LT(L[1], R[1]), k2 = LT(L[2], R[2]), k3 = LT(L[3], R[3]);")
-    w("    const bool i1 = in_slab(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], s1[6], ctx);")
-    w("    const bool i2 = in_slab(s2[0], s2[1], s2[2], s2[3], s2[4], s2[5], s2[6], ctx);")
-    w("    hit = j < 16 && k0 && k1 && (k2 || i1) && (k3 || i2);")
+    w("    /* every part evaluated on every lane (all are pure), each with its own context */")
+    w("    C c0 = ctx, c1 = ctx, c2 = ctx, c3 = ctx, ci1 = ctx, ci2 = ctx, ce = ctx;")
+    w("    const bool k0 = cmp_lt(L[0], R[0], c0, 0), k1 = cmp_lt(L[1], R[1], c1, 0);")
+    w("    const bool k2 = cmp_lt(L[2], R[2], c2, 0), k3 = cmp_lt(L[3], R[3], c3, 0);")
+    w("    const bool i1 = in_slab(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], s1[6], ci1);")
+    w("    const bool i2 = in_slab(s2[0], s2[1], s2[2], s2[3], s2[4], s2[5], s2[6], ci2);")
+    w("    const int t0 = c0.bad ? -1 : k0, t1 = c1.bad ? -1 : k1, t2 = c2.bad ? -1 : k2, t3 = c3.bad ? -1 : k3;")
+    w("    const int u1 = ci1.bad ? -1 : i1, u2 = ci2.bad ? -1 : i2;")
+    w("    hit = (j < 16 && !ctx.bad) ? rc_and3(rc_and3(t0, t1), rc_and3(rc_or3(t2, u1), rc_or3(t3, u2))) : (ctx.bad ? -1 : 0);")
     w("    T t, u;")
-    w("    edge_params(t, u, e[0], e[1], e[2], e[3], e[4], ctx);")
+    w("    edge_params(t, u, e[0], e[1], e[2], e[3], e[4], ce);")
     w("    const T Px = px == 0 ? a[0] : px == 1 ? a[1] : px == 4 ? t : zero;")
     w("    const T Py = py == 0 ? a[0] : py == 1 ? a[1] : py == 4 ? t : zero;")
     w("    const V3T<T> P = v3t<T>(Px, Py, zero);")
@@ -187,6 +198,7 @@ def main():
     w("    const V3T<T> Q1 = v3t(Tab.x + rux * u, Tab.y + ruy * u, Tab.z + ruz * u);")
     w("    const V3T<T> Q = qkind == 2 ? Q2 : Q1;")
     w("    S = v3t(Q.x - P.x, Q.y - P.y, Q.z - P.z);")
+    w("    vbad = ce.bad;")
     w("    return num_sqrt(dot(S, S));")
     w("}")
     w("")

@@ -24,7 +24,7 @@ def main():
     ap.add_argument("--slots", type=int, default=64)
     ap.add_argument("--pick", type=str, default="")
     ap.add_argument("--mode", choices=["reference", "canonical"], default="reference")
-    ap.add_argument("--engine", choices=["auto", "warp", "batched"], default="auto")
+    ap.add_argument("--engine", choices=["auto", "warp", "batched", "thread"], default="auto")
     args = ap.parse_args()
 
     import torch
@@ -37,8 +37,8 @@ def main():
         wl = wl.subset(np.array([int(i) for i in args.pick.split(",")]))
     if args.mode == "canonical":
         wl.params["mode"] = api.MODE_CANONICAL
-        wl.params["engine"] = {"auto": api.ENGINE_AUTO, "warp": api.ENGINE_WARP,
-                               "batched": api.ENGINE_BATCHED}[args.engine]
+    wl.params["engine"] = {"auto": api.ENGINE_AUTO, "warp": api.ENGINE_WARP, "batched": api.ENGINE_BATCHED,
+                           "thread": api.ENGINE_THREAD}[args.engine]
     ctx = api.Context(0)
     mid = ctx.model(wl.meshes[0])
     q = wl.qint.copy()

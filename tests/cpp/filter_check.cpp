@@ -222,9 +222,10 @@ int c2a_fc_rect_lanes(const double *Rab9, const double *Tab3, const double *a, c
     V3 Sw = v3(0, 0, 0);
     for (int j = 0; j < 16; j++) {
         V3 Sj;
-        bool hit = false;
-        const double dj = rect_case(j, R, T, a, b, Sj, hit, xc);
-        if (hit) {
+        int hit = 0;
+        bool vbad = false;
+        const double dj = rect_case(j, R, T, a, b, Sj, hit, vbad, xc);
+        if (hit == 1) {
             win = j;
             d = dj;
             Sw = Sj;

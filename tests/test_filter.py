@@ -106,3 +106,30 @@ def test_filter_bounds_hold_small_knots(fc):
     rec = _walk(fc, wl.meshes[0], wl.poses, 8, np.random.default_rng(6))
     assert not rec["viol"], rec["viol"][:3]
     assert rec["bv_ok"] >= 0.95 * rec["bv"], rec
+
+
+def test_rect_cases_lane_parallel_match_sequential(fc):
+    """rect_cases.cuh (C2ARectDist's 16 cases evaluated independently, the
+    first that holds wins, else the face-separation tail) against the
+    sequential rect_dist and the reference's own RectDist outputs, bit for bit."""
+    from c2a_testutil import GOLDEN
+
+    fc.c2a_fc_rect_lanes.argtypes = [C.c_void_p] * 5
+    z = np.load(os.path.join(GOLDEN, "geometry_ref.npz"))
+    out = np.zeros(9)
+    for i in range(len(z["rect_d"])):
+        fc.c2a_fc_rect_lanes(_p(z["Rab"][i]), _p(z["Tab"][i]), _p(z["a"][i]), _p(z["b"][i]), _p(out))
+        assert out[4].tobytes() == np.float64(z["rect_d"][i]).tobytes(), i
+        assert out[0].tobytes() == out[4].tobytes() and out[1:4].tobytes() == out[5:8].tobytes(), i
+    rng = np.random.default_rng(7)
+    Rs = workloads.random_rotations(rng, 20000).reshape(-1, 9)
+    cases = set()
+    for i in range(20000):
+        R = Rs[i] if i % 5 else np.round(Rs[i] * 2) / 2  # also near-axis-aligned, degenerate frames
+        T = rng.normal(size=3) * rng.choice([0.01, 0.3, 2.0])
+        a = rng.uniform(0, 1, 2) * (rng.random(2) > 0.05)
+        b = rng.uniform(0, 1, 2) * (rng.random(2) > 0.05)
+        fc.c2a_fc_rect_lanes(_p(R), _p(T), _p(a), _p(b), _p(out))
+        assert out[0].tobytes() == out[4].tobytes() and out[1:4].tobytes() == out[5:8].tobytes(), i
+        cases.add(int(out[8]))
+    assert cases == set(range(-1, 16)), sorted(cases)
