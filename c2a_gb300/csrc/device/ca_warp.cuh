@@ -353,6 +353,46 @@ C2A_KDEV void split_pair(const Query &q, int b1, int b2, int fc1, int fc2, int &
     }
 }
 
+C2A_KDEV double pick3(double a, double b, double c, int i) { return i == 0 ? a : (i == 1 ? b : c); }
+
+/* child_transform on one half-warp: lane k < 9 of the half computes R[k / 3][k % 3],
+ * lanes 9..11 T[k - 9], with the expression trees of tmmul/tmul (side 0) or
+ * mmul/mul_add (side 1); the half then shares the twelve values */
+C2A_KDEV void child_transform_lanes(const Query &q, int side, int x1, int x2, const M3 &PR, V3 PT, M3 &R, V3 &T,
+                                    int lane)
+{
+    const int half = lane >> 4, k = lane & 15;
+    const NodeRec *n = side == 0 ? q.A->nodes + x1 : q.B->nodes + x2;
+    const M3 Rc = load_R(n);
+    const V3 Tr = load_Tr(n);
+    const bool isT = k >= 9;
+    const int i = isT ? (k - 9 < 3 ? k - 9 : 2) : k / 3, j = isT ? 0 : k % 3;
+    double a0, a1, a2, b0, b1, b2, c = 0.0;
+    if (side == 0) { /* R = Rc^T PR, T = Rc^T (PT - Tr) */
+        a0 = pick3(Rc.m[0], Rc.m[1], Rc.m[2], i);
+        a1 = pick3(Rc.m[3], Rc.m[4], Rc.m[5], i);
+        a2 = pick3(Rc.m[6], Rc.m[7], Rc.m[8], i);
+        const V3 v = PT - Tr;
+        b0 = isT ? v.x : pick3(PR.m[0], PR.m[1], PR.m[2], j);
+        b1 = isT ? v.y : pick3(PR.m[3], PR.m[4], PR.m[5], j);
+        b2 = isT ? v.z : pick3(PR.m[6], PR.m[7], PR.m[8], j);
+    } else { /* R = PR Rc, T = PR Tr + PT */
+        a0 = pick3(PR.m[0], PR.m[3], PR.m[6], i);
+        a1 = pick3(PR.m[1], PR.m[4], PR.m[7], i);
+        a2 = pick3(PR.m[2], PR.m[5], PR.m[8], i);
+        b0 = isT ? Tr.x : pick3(Rc.m[0], Rc.m[1], Rc.m[2], j);
+        b1 = isT ? Tr.y : pick3(Rc.m[3], Rc.m[4], Rc.m[5], j);
+        b2 = isT ? Tr.z : pick3(Rc.m[6], Rc.m[7], Rc.m[8], j);
+        c = pick3(PT.x, PT.y, PT.z, i);
+    }
+    double v = a0 * b0 + a1 * b1 + a2 * b2;
+    if (side == 1 && isT) v = v + c;
+    const int base = 16 * half;
+#pragma unroll
+    for (int e = 0; e < 9; e++) R.m[e] = shfl_d(v, base + e);
+    T = v3(shfl_d(v, base + 9), shfl_d(v, base + 10), shfl_d(v, base + 11));
+}
+
 /* bv_test_x of child pair (x1, x2) placed by (R, T), exactly, on one half-warp */
 C2A_KDEV void child_test_x(const Query &q, int x1, int x2, const M3 &R, V3 T, double &d, double &mint, int lane)
 {
@@ -364,13 +404,19 @@ C2A_KDEV void child_test_x(const Query &q, int x1, int x2, const M3 &R, V3 T, do
     z -= (n1.r + n2.r);
     d = max0_c(z);
     mint = 0.0;
-    if (d != 0.0 && q.want_mint) {
+    if (q.want_mint) { /* uniform over the warp; d differs between the halves */
+        /* the two motion bounds on alternate lanes of the half, then shared; every
+         * lane computes one (the shuffles need the whole warp), the result is
+         * used where the reference computes it (d != 0) */
         ExactCtx xc{false};
-        V3 S1 = mul(q.r1, mul(n1.Rloc, S));
-        V3 S2 = mul_s(S1, -1.0);
-        const double mb1 = bound_rss(q.x1, n1.angR, S1, xc);
-        const double mb2 = bound_rss(q.x2, n2.angR, S2, xc);
-        mint = max0_c((d) / (mb1 + mb2));
+        const V3 S1 = mul(q.r1, mul(n1.Rloc, S));
+        const bool second = (lane & 1) != 0;
+        V3 N = second ? mul_s(S1, -1.0) : S1;
+        const MotionT<double> mm = second ? q.x2 : q.x1;
+        const double mb = bound_rss(mm, second ? n2.angR : n1.angR, N, xc);
+        const int base = 16 * (lane >> 4);
+        const double mb1 = shfl_d(mb, base), mb2 = shfl_d(mb, base + 1);
+        if (d != 0.0) mint = max0_c((d) / (mb1 + mb2));
     }
 }
 
@@ -440,7 +486,7 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
     const int x1 = half ? c1 : a1, x2 = half ? c2 : a2;
     M3 R;
     V3 T;
-    child_transform(q, side, x1, x2, PR, PT, R, T);
+    child_transform_lanes(q, side, x1, x2, PR, PT, R, T, lane);
     EF d = ef_exact(0.0f), m = ef_exact(0.0f);
     bool d_zero = false;
     const bool ok = C2A_WARP_FILTER && child_test_e(q, x1, x2, R, T, d, m, d_zero, lane);
