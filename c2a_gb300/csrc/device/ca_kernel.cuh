@@ -45,12 +45,21 @@ enum {
     ST_EXPAND, ST_BVE, ST_BVE_FAIL, ST_BVE_ZERO, ST_EX_DESCEND, ST_EX_CONTRIB, ST_EX_ORDER, ST_LEAF,
     ST_LEAF_SKIP, ST_LEAF_EXACT, ST_LEAF_IMPROVE, ST_NO_SHADOW, ST_EXACT, ST_STEP, ST_CLEAF, ST_CLEAF_EXACT,
     ST_D_ROUNDS, ST_D_POPS, ST_D_LEAF_EXACT, ST_D_KCYC, ST_T_ROUNDS, ST_T_POPS, ST_T_KCYC, ST_C_KCYC, ST_Q_KCYC,
+    /* the warp kernel: events and clock64 cycles per phase (64-bit, per query in wst) */
+    ST_W_EXPAND, ST_W_EFAIL, ST_W_MKEXACT, ST_W_LEAF, ST_W_LEAF_X, ST_W_CYC_XFORM, ST_W_CYC_TEST_E,
+    ST_W_CYC_TEST_X, ST_W_CYC_STORE, ST_W_CYC_DECIDE, ST_W_CYC_LEAF, ST_W_CYC_DFS, ST_W_CYC_QUERY,
+    ST_W_CYC_X_RECT, ST_W_CYC_X_BOUND, ST_W_CYC_E_RECT, ST_W_CYC_E_BOUND,
     ST_COUNT
 };
+constexpr int ST_W_FIRST = ST_W_EXPAND;
 static __device__ unsigned long long g_c2a_stats[ST_COUNT];
 #define C2A_STAT(q, i) ((q).st[i]++)
+#define C2A_WSTAT(q, i, x) ((q).wst[(i) - ST_W_FIRST] += (unsigned long long)(x))
+#define C2A_WCLOCK(v) const long long v = clock64()
 #else
 #define C2A_STAT(q, i) ((void)0)
+#define C2A_WSTAT(q, i, x) ((void)0)
+#define C2A_WCLOCK(v) ((void)0)
 #endif
 
 struct DevModel {
@@ -181,8 +190,10 @@ struct Query {
     EF rel1_e;                                 /* 1 + rel_err (1, 4 or 1.5: exact in FP32) */
     bool shadows_ok;
     bool want_mint;                            /* BV tests also bound the motion (not for contacts) */
+    double *rt;                                /* the warp kernel's RectDist slots for this half-warp */
 #ifdef C2A_STATS
     mutable unsigned int st[ST_COUNT];
+    mutable unsigned long long wst[ST_COUNT - ST_W_FIRST];
 #endif
     long long nbv, ntri;
     int numCA;

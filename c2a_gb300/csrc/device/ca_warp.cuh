@@ -26,6 +26,7 @@
 
 #include "ca_kernel.cuh"
 #include "rect_cases.cuh"
+#include "rect_table.cuh"
 
 namespace c2a {
 
@@ -52,6 +53,7 @@ struct WStackEntry {
 struct WarpShared {
     WStackEntry stack[C2A_STACK_DEPTH];
     WStackEntry child[2]; /* the children of the pair just expanded */
+    double rt[2][64];     /* each half's RectDist slots (rect_table.cuh) */
 };
 
 C2A_KDEV double shfl_d(double v, int src) { return __shfl_sync(kWFull, v, src); }
@@ -313,18 +315,35 @@ C2A_KDEV EF tri_distance_warp_e(const Query &q, int ia, int ib, TriFeat &f, bool
 
 /* ------------------------------------------------------- child pair tests */
 
-/* C2A_BV_Distance of this half-warp's child pair (x1, x2) placed by (R, T):
- * the rectangle distance with its S, on the half's sixteen lanes */
-C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const double b[2], V3 &S, int lane)
+/* C2A_BV_Distance of this half-warp's child pair placed by (R, T): the
+ * rectangle distance with its S, on the half's sixteen lanes.  The shared
+ * sums are spread over the lanes (slots V in shared memory, rect_table.cuh),
+ * lane j then tests edge-pair case j; the first case that holds wins and only
+ * its lane evaluates the distance; no case: the face-separation tail. */
+C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const double b[2], V3 &S, double *V, int lane)
 {
-    ExactCtx xc{false};
-    const int half = lane >> 4, j = lane & 15;
-    V3 Sj = v3(0, 0, 0);
-    int hit = 0;
-    bool vbad = false;
-    const double dj = rect_case(j, R, T, a, b, Sj, hit, vbad, xc);
-    const unsigned m = (__ballot_sync(kWFull, hit == 1) >> (16 * half)) & 0xffffu;
+    const int half = lane >> 4, k = lane & 15;
+    __syncwarp(); /* the previous call's reads of V are done */
+    if (k < kRtInputs) V[k] = rt_input(k, R, T, a, b);
+    if (k < kRtStage1) V[kRtInputs + k] = rt_stage1(k, R, T, a, b);
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const int i = k + 16 * r;
+        if (i < kRtStage2) V[kRtStage2Base + i] = rt_stage2(i, V);
+    }
+    __syncwarp();
+    const bool below = k < 8 && rt_compare(k, V);
+    const unsigned mask = (__ballot_sync(kWFull, below) >> (16 * half)) & 0xffu;
+    double L[4], Rr[4], s1[7], s2[7], e[5], qb;
+    int px, py, qkind, cb, cu;
+    rt_case_operands(k, mask, V, L, Rr, s1, s2, e, qb, px, py, qkind, cb, cu);
+    const bool hit = rt_case_holds(L, Rr, s1, s2);
+    const unsigned m = (__ballot_sync(kWFull, hit) >> (16 * half)) & 0xffffu;
     const int win = m ? __ffs(m) - 1 : 0;
+    double dj = 0.0;
+    V3 Sj = v3(0, 0, 0);
+    if (m && k == win) dj = rt_case_value(e, qb, px, py, qkind, cb, cu, R, T, a, Sj);
     const int src = 16 * half + win;
     const double dw = shfl_d(dj, src);
     const V3 Sw = shfl_v3(Sj, src);
@@ -332,6 +351,7 @@ C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const doubl
         S = Sw;
         return dw;
     }
+    ExactCtx xc{false};
     V3 St = S; /* the tail leaves S untouched when both separations are negative */
     const double dt = rect_tail(R, T, a, b, St, xc);
     S = St;
@@ -400,23 +420,32 @@ C2A_KDEV void child_test_x(const Query &q, int x1, int x2, const M3 &R, V3 T, do
     load_x(n1, q.A->nodes + x1);
     load_x(n2, q.B->nodes + x2);
     V3 S = v3(0, 0, 0);
-    double z = rect_dist_half(R, T, n1.l, n2.l, S, lane);
+    C2A_WCLOCK(xc0);
+    double z = rect_dist_half(R, T, n1.l, n2.l, S, q.rt, lane);
+    C2A_WCLOCK(xc1);
+    C2A_WSTAT(q, ST_W_CYC_X_RECT, xc1 - xc0);
     z -= (n1.r + n2.r);
     d = max0_c(z);
     mint = 0.0;
     if (q.want_mint) { /* uniform over the warp; d differs between the halves */
-        /* the two motion bounds on alternate lanes of the half, then shared; every
-         * lane computes one (the shuffles need the whole warp), the result is
-         * used where the reference computes it (d != 0) */
+        /* S1 = r1 (Rloc S) one row per lane, then the two motion bounds on
+         * alternate lanes of the half, then shared; every lane computes (the
+         * shuffles need the whole warp), the result is used where the reference
+         * computes it (d != 0) */
         ExactCtx xc{false};
-        const V3 S1 = mul(q.r1, mul(n1.Rloc, S));
+        const int base = 16 * (lane >> 4), row = (lane & 15) % 3;
+        const double u = n1.Rloc.m[3 * row] * S.x + n1.Rloc.m[3 * row + 1] * S.y + n1.Rloc.m[3 * row + 2] * S.z;
+        const V3 U = v3(shfl_d(u, base), shfl_d(u, base + 1), shfl_d(u, base + 2));
+        const double w = q.r1.m[3 * row] * U.x + q.r1.m[3 * row + 1] * U.y + q.r1.m[3 * row + 2] * U.z;
+        const V3 S1 = v3(shfl_d(w, base), shfl_d(w, base + 1), shfl_d(w, base + 2));
         const bool second = (lane & 1) != 0;
         V3 N = second ? mul_s(S1, -1.0) : S1;
         const MotionT<double> mm = second ? q.x2 : q.x1;
         const double mb = bound_rss(mm, second ? n2.angR : n1.angR, N, xc);
-        const int base = 16 * (lane >> 4);
         const double mb1 = shfl_d(mb, base), mb2 = shfl_d(mb, base + 1);
         if (d != 0.0) mint = max0_c((d) / (mb1 + mb2));
+        C2A_WCLOCK(xc2);
+        C2A_WSTAT(q, ST_W_CYC_X_BOUND, xc2 - xc1);
     }
 }
 
@@ -435,6 +464,7 @@ C2A_KDEV bool child_test_e(const Query &q, int x1, int x2, const M3 &R, V3 T, EF
     V3T<EF> Sj = v3t(zero, zero, zero);
     int hit = 0;
     bool vbad = false;
+    C2A_WCLOCK(y0);
     const EF dj = rect_case(j, Re, Te, n1.l, n2.l, Sj, hit, vbad, pc);
     const unsigned nz = (__ballot_sync(kWFull, hit != 0) >> (16 * half)) & 0xffffu;
     const int src = 16 * half + (nz ? __ffs(nz) - 1 : 0);
@@ -456,6 +486,8 @@ C2A_KDEV bool child_test_e(const Query &q, int x1, int x2, const M3 &R, V3 T, EF
         S = St;
         ok = !tc.bad;
     }
+    C2A_WCLOCK(y1);
+    C2A_WSTAT(q, ST_W_CYC_E_RECT, y1 - y0);
     const EF z = dist - (n1.r + n2.r);
     const int pos = ef_lt3(zero, z);
     if (pos < 0) ok = false;
@@ -471,6 +503,8 @@ C2A_KDEV bool child_test_e(const Query &q, int x1, int x2, const M3 &R, V3 T, EF
         mint = max0_c(ef_div(d, mb1 + mb2, bc));
         ok = !bc.bad;
     }
+    C2A_WCLOCK(y2);
+    C2A_WSTAT(q, ST_W_CYC_E_BOUND, y2 - y1);
     return ok;
 }
 
@@ -486,16 +520,25 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
     const int x1 = half ? c1 : a1, x2 = half ? c2 : a2;
     M3 R;
     V3 T;
+    C2A_WCLOCK(w0);
     child_transform_lanes(q, side, x1, x2, PR, PT, R, T, lane);
+    C2A_WCLOCK(w1);
     EF d = ef_exact(0.0f), m = ef_exact(0.0f);
     bool d_zero = false;
     const bool ok = C2A_WARP_FILTER && child_test_e(q, x1, x2, R, T, d, m, d_zero, lane);
+    C2A_WCLOCK(w2);
     double dx = 0.0, mx = 0.0;
     int exact = d_zero ? 1 : 0; /* d = max(z, 0) = 0 and mint = 0 exactly */
     if (!__all_sync(kWFull, ok)) {
         child_test_x(q, x1, x2, R, T, dx, mx, lane);
         exact = 1;
+        C2A_WSTAT(q, ST_W_EFAIL, 1);
     }
+    C2A_WCLOCK(w3);
+    C2A_WSTAT(q, ST_W_EXPAND, 1);
+    C2A_WSTAT(q, ST_W_CYC_XFORM, w1 - w0);
+    C2A_WSTAT(q, ST_W_CYC_TEST_E, w2 - w1);
+    C2A_WSTAT(q, ST_W_CYC_TEST_X, w3 - w2);
     if ((lane & 15) == 0) {
         WStackEntry &e = sh.child[half];
         e.b1 = x1;
@@ -516,12 +559,15 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
         e.T = T;
     }
     __syncwarp();
+    C2A_WCLOCK(w4);
+    C2A_WSTAT(q, ST_W_CYC_STORE, w4 - w3);
 }
 
 /* the exact d and mint of a child pair (both halves compute it; uniform) */
 C2A_KDEV void make_exact_warp(const Query &q, WStackEntry &e, int lane)
 {
     if (e.exact) return;
+    C2A_WSTAT(q, ST_W_MKEXACT, 1);
     child_test_x(q, e.b1, e.b2, e.R, e.T, e.d, e.m, lane);
     EFCtx cc{false};
     e.d_e = in_d(e.d, cc);
@@ -572,6 +618,7 @@ C2A_KDEV void leaf_step_warp(Query &q, int b1, int b2, int fc1, int fc2, int lan
 {
     const int ia = -fc1 - 1, ib = -fc2 - 1;
     q.ntri++;
+    C2A_WSTAT(q, ST_W_LEAF, 1);
     if (C2A_WARP_FILTER && q.shadows_ok) { /* most leaves cannot reach the running distance */
         TriFeat fe;
         bool ok = false;
@@ -581,6 +628,7 @@ C2A_KDEV void leaf_step_warp(Query &q, int b1, int b2, int fc1, int fc2, int lan
     V3 p, qq;
     TriFeat f;
     bool col = false;
+    C2A_WSTAT(q, ST_W_LEAF_X, 1);
     const double dTri = tri_distance_warp(q, ia, ib, p, qq, f, col, lane);
     if (dTri <= q.distance) {
         ExactCtx xc{false};
@@ -609,13 +657,17 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
         const int fc1 = __ldg(&q.A->nodes[b1].first_child), fc2 = __ldg(&q.B->nodes[b2].first_child);
         bool go = false;
         if (fc1 < 0 && fc2 < 0) {
+            C2A_WCLOCK(l0);
             leaf_step_warp(q, b1, b2, fc1, fc2, lane);
+            C2A_WCLOCK(l1);
+            C2A_WSTAT(q, ST_W_CYC_LEAF, l1 - l0);
         } else {
             if (sp >= C2A_STACK_DEPTH) {
                 q.status |= C2A_QUERY_STACK_OVERFLOW;
                 return;
             }
             expand_warp(q, b1, b2, fc1, fc2, R, T, sh, lane);
+            C2A_WCLOCK(k0);
             q.nbv += 2;
             WStackEntry a = sh.child[0], c = sh.child[1];
             const bool c_first = closer_second_w(q, a, c, lane);
@@ -632,7 +684,10 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
                 contribute_w(q, first, lane);
             }
             __syncwarp();
+            C2A_WCLOCK(k1);
+            C2A_WSTAT(q, ST_W_CYC_DECIDE, k1 - k0);
         }
+        C2A_WCLOCK(p0);
         while (!go && sp > 0) {
             WStackEntry e = sh.stack[--sp];
             if (descend_w(q, e, lane)) {
@@ -646,6 +701,8 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
             }
         }
         __syncwarp();
+        C2A_WCLOCK(p1);
+        C2A_WSTAT(q, ST_W_CYC_DECIDE, p1 - p0);
         if (!go) return;
     }
 }
@@ -672,7 +729,10 @@ C2A_KDEV void toc_step_warp(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, WarpShared
     }
     q.mint = 1;
     refresh_shadows(q);
+    C2A_WCLOCK(d0);
     toc_dfs_warp(q, R, T, sh, lane);
+    C2A_WCLOCK(d1);
+    C2A_WSTAT(q, ST_W_CYC_DFS, d1 - d0);
 }
 
 /* --------------------------------------------------- contact enumeration */
@@ -806,11 +866,14 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
     Query q;
 #ifdef C2A_STATS
     for (int i = 0; i < ST_COUNT; i++) q.st[i] = 0;
+    for (int i = 0; i < ST_COUNT - ST_W_FIRST; i++) q.wst[i] = 0;
+    C2A_WCLOCK(qc0);
 #endif
     q.status = 0;
     q.A = models + in.model_a;
     q.B = models + in.model_b;
     q.want_mint = true;
+    q.rt = sh.rt[lane >> 4];
     const double *P = in.pose;
     set_motions(q, P);
     q.toc_delta = prm.toc_delta;
@@ -917,6 +980,12 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
     }
     out.status |= q.status;
     if (lane == 0) out_g = out;
+#ifdef C2A_STATS
+    C2A_WCLOCK(qc1);
+    C2A_WSTAT(q, ST_W_CYC_QUERY, qc1 - qc0);
+    if (lane == 0)
+        for (int i = ST_W_FIRST; i < ST_COUNT; i++) atomicAdd(&g_c2a_stats[i], q.wst[i - ST_W_FIRST]);
+#endif
 }
 
 } // namespace c2a

@@ -14,6 +14,7 @@
 
 #include "../../c2a_gb300/csrc/device/geom.cuh"
 #include "../../c2a_gb300/csrc/device/rect_cases.cuh"
+#include "../../c2a_gb300/csrc/device/rect_table.cuh"
 
 using namespace c2a;
 
@@ -236,6 +237,44 @@ int c2a_fc_rect_lanes(const double *Rab9, const double *Tab3, const double *a, c
     out[4] = d;
     out[5] = Sw.x; out[6] = Sw.y; out[7] = Sw.z;
     out[8] = win;
+    return 0;
+}
+
+/*
+ * rect_table.cuh (the half-warp form: slots computed a few per lane, the
+ * eight sort comparisons as a mask, operands through the table), emulated
+ * lane by lane.  out: d, S[3], winning case (-1: tail).
+ */
+int c2a_fc_rect_table(const double *Rab9, const double *Tab3, const double *a, const double *b, double *out)
+{
+    const M3 R = m3_of(Rab9);
+    const V3 T = v3(Tab3[0], Tab3[1], Tab3[2]);
+    double V[64];
+    for (int k = 0; k < kRtInputs; k++) V[k] = rt_input(k, R, T, a, b);
+    for (int k = 0; k < kRtStage1; k++) V[kRtInputs + k] = rt_stage1(k, R, T, a, b);
+    for (int i = 0; i < kRtStage2; i++) V[kRtStage2Base + i] = rt_stage2(i, V);
+    unsigned mask = 0;
+    for (int g = 0; g < 8; g++)
+        if (rt_compare(g, V)) mask |= 1u << g;
+    int win = -1;
+    double d = 0.0;
+    V3 S = v3(0, 0, 0);
+    for (int j = 0; j < 16 && win < 0; j++) {
+        double L[4], Rr[4], s1[7], s2[7], e[5], qb;
+        int px, py, qkind, cb, cu;
+        rt_case_operands(j, mask, V, L, Rr, s1, s2, e, qb, px, py, qkind, cb, cu);
+        if (rt_case_holds(L, Rr, s1, s2)) {
+            win = j;
+            d = rt_case_value(e, qb, px, py, qkind, cb, cu, R, T, a, S);
+        }
+    }
+    if (win < 0) {
+        ExactCtx xc{false};
+        d = rect_tail(R, T, a, b, S, xc);
+    }
+    out[0] = d;
+    out[1] = S.x; out[2] = S.y; out[3] = S.z;
+    out[4] = win;
     return 0;
 }
 

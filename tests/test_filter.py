@@ -110,17 +110,23 @@ def test_filter_bounds_hold_small_knots(fc):
 
 def test_rect_cases_lane_parallel_match_sequential(fc):
     """rect_cases.cuh (C2ARectDist's 16 cases evaluated independently, the
-    first that holds wins, else the face-separation tail) against the
-    sequential rect_dist and the reference's own RectDist outputs, bit for bit."""
+    first that holds wins, else the face-separation tail) and rect_table.cuh
+    (the same with the shared sums spread over lanes and the operands read
+    through tables) against the sequential rect_dist and the reference's own
+    RectDist outputs, bit for bit."""
     from c2a_testutil import GOLDEN
 
     fc.c2a_fc_rect_lanes.argtypes = [C.c_void_p] * 5
+    fc.c2a_fc_rect_table.argtypes = [C.c_void_p] * 5
     z = np.load(os.path.join(GOLDEN, "geometry_ref.npz"))
     out = np.zeros(9)
+    tab = np.zeros(5)
     for i in range(len(z["rect_d"])):
         fc.c2a_fc_rect_lanes(_p(z["Rab"][i]), _p(z["Tab"][i]), _p(z["a"][i]), _p(z["b"][i]), _p(out))
+        fc.c2a_fc_rect_table(_p(z["Rab"][i]), _p(z["Tab"][i]), _p(z["a"][i]), _p(z["b"][i]), _p(tab))
         assert out[4].tobytes() == np.float64(z["rect_d"][i]).tobytes(), i
         assert out[0].tobytes() == out[4].tobytes() and out[1:4].tobytes() == out[5:8].tobytes(), i
+        assert tab[:4].tobytes() == out[4:8].tobytes() and tab[4] == out[8], i
     rng = np.random.default_rng(7)
     Rs = workloads.random_rotations(rng, 20000).reshape(-1, 9)
     cases = set()
@@ -130,6 +136,8 @@ def test_rect_cases_lane_parallel_match_sequential(fc):
         a = rng.uniform(0, 1, 2) * (rng.random(2) > 0.05)
         b = rng.uniform(0, 1, 2) * (rng.random(2) > 0.05)
         fc.c2a_fc_rect_lanes(_p(R), _p(T), _p(a), _p(b), _p(out))
+        fc.c2a_fc_rect_table(_p(R), _p(T), _p(a), _p(b), _p(tab))
         assert out[0].tobytes() == out[4].tobytes() and out[1:4].tobytes() == out[5:8].tobytes(), i
+        assert tab[:4].tobytes() == out[4:8].tobytes() and tab[4] == out[8], i
         cases.add(int(out[8]))
     assert cases == set(range(-1, 16)), sorted(cases)
