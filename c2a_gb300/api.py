@@ -27,7 +27,11 @@ CONTACT_DTYPE = np.dtype([("type_a", np.int32), ("type_b", np.int32), ("fid_a", 
                           ("fid_b", np.int32, (3,)), ("tri_a", np.int32), ("tri_b", np.int32),
                           ("query", np.int32), ("pad", np.int32), ("pa", np.float64, (3,)),
                           ("pb", np.float64, (3,)), ("distance", np.float64)], align=True)
+DISTANCE_DTYPE = np.dtype([("distance", np.float64), ("p1", np.float64, (3,)), ("p2", np.float64, (3,)),
+                           ("tri_a", np.int32), ("tri_b", np.int32), ("status", np.int32), ("pad", np.int32)],
+                          align=True)
 assert QUERY_DTYPE.itemsize == 400 and RESULT_DTYPE.itemsize == 264 and CONTACT_DTYPE.itemsize == 104
+assert DISTANCE_DTYPE.itemsize == 72
 
 C2A_OK = 0
 QUERY_BAD_INPUT, QUERY_STACK_OVERFLOW, QUERY_CONTACT_OVERFLOW, QUERY_ITER_CAP = 1, 2, 4, 8
@@ -36,6 +40,7 @@ QUERY_BAD_INPUT, QUERY_STACK_OVERFLOW, QUERY_CONTACT_OVERFLOW, QUERY_ITER_CAP = 
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
                "c2a_model_info", "c2a_model_download", "c2a_model_free", "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
+               "c2a_distance_batch",
                "c2a_motion_setup", "c2a_motion_integrate"]
 
 
@@ -105,6 +110,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_solve_batch_noalloc": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp], i32),
         "c2a_toc_step_batch": ([vp, vp, i32, vp, vp, vp, C.POINTER(Params), vp], i32),
         "c2a_contact_only_batch": ([vp, vp, i32, vp, i32, vp, vp], i32),
+        "c2a_distance_batch": ([vp, vp, i32, vp], i32),
         "c2a_motion_setup": ([vp, vp, vp, vp, vp], i32),
         "c2a_motion_integrate": ([vp, vp, vp, vp, dbl, vp, vp, vp], i32),
     }
@@ -235,6 +241,16 @@ class Context:
         if check:
             _check(s, "c2a_solve_batch")
         return res, Contacts(con, res, contacts_per_query)
+
+    def distance(self, qint: np.ndarray, poses: np.ndarray, check: bool = True) -> np.ndarray:
+        """C2A_Distance (rel_err = abs_err = 0) for a batch: model_a at pose[0:12],
+        model_b at pose[24:36], seeded with (seed_a, seed_b); DISTANCE_DTYPE rows."""
+        q = make_queries(qint, poses)
+        res = np.zeros(len(q), dtype=DISTANCE_DTYPE)
+        s = self.lib.c2a_distance_batch(self.h, _ptr(q), len(q), _ptr(res))
+        if check:
+            _check(s, "c2a_distance_batch")
+        return res
 
     def solve_device(self, d_queries: int, n: int, params: dict, d_results: int, d_contacts: int | None,
                      contacts_per_query: int, stream: int | None = None):

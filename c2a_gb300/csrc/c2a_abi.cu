@@ -84,6 +84,7 @@ struct c2a_context {
     size_t order_cap = 0;
     int canonical_blocks_per_sm = 0;
     int warp_blocks_per_sm = 0;
+    int distance_blocks_per_sm = 0;
     std::mutex mu;
 };
 
@@ -136,6 +137,21 @@ c2a_status ensure_buf(c2a_context *ctx, size_t bytes)
     size_t sz = bytes + bytes / 4 + 4096;
     C2A_CUDA(cudaMalloc(&ctx->d_buf, sz));
     ctx->d_buf_size = sz;
+    return C2A_OK;
+}
+
+/* front slices for `warps` warps (allocates `want` >= warps when it grows) */
+c2a_status ensure_fronts(c2a_context *ctx, size_t warps, size_t want)
+{
+    if (warps <= ctx->fronts_warps) return C2A_OK;
+    /* a stream may still read the old slices: wait before freeing */
+    C2A_CUDA(cudaDeviceSynchronize());
+    if (ctx->d_fronts) cudaFree(ctx->d_fronts);
+    ctx->d_fronts = nullptr;
+    ctx->fronts_warps = 0;
+    if (want < warps) want = warps;
+    C2A_CUDA(cudaMalloc(&ctx->d_fronts, want * (size_t)C2A_FRONT_CAP * sizeof(Pending)));
+    ctx->fronts_warps = want;
     return C2A_OK;
 }
 
@@ -383,6 +399,26 @@ __global__ void __launch_bounds__(kThreads) c2a_canonical_kernel(const c2a_query
         c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
         solve_query_canonical(queries[q], models, num_models, prm, results[q], cq, stack, C2A_FRONT_CAP, lane,
                               (int)q);
+    }
+}
+
+/* C2A_Distance for a batch: one warp per pair (persistent), each with its own
+ * slice of the front buffer */
+__global__ void __launch_bounds__(kThreads) c2a_distance_kernel(const c2a_query *__restrict__ queries, int n,
+                                                                const DevModel *__restrict__ models, int num_models,
+                                                                c2a_distance_result *__restrict__ results,
+                                                                unsigned int *__restrict__ counter,
+                                                                Pending *__restrict__ fronts)
+{
+    const int lane = threadIdx.x & 31;
+    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    Pending *stack = fronts + warp * (size_t)C2A_FRONT_CAP;
+    for (;;) {
+        unsigned int q = 0;
+        if (lane == 0) q = atomicAdd(counter, 1u);
+        q = __shfl_sync(kFullMask, q, 0);
+        if (q >= (unsigned int)n) break;
+        distance_query_warp(queries[q], models, num_models, results[q], stack, C2A_FRONT_CAP, lane);
     }
 }
 
@@ -682,17 +718,8 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
         const int most = ctx->sm_count * ctx->canonical_blocks_per_sm;
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
         const int blocks = need < most ? need : most;
-        const size_t warps = (size_t)blocks * (kThreads / 32);
-        if (warps > ctx->fronts_warps) {
-            /* a stream may still read the old slices: wait before freeing */
-            C2A_CUDA(cudaDeviceSynchronize());
-            if (ctx->d_fronts) cudaFree(ctx->d_fronts);
-            ctx->d_fronts = nullptr;
-            ctx->fronts_warps = 0;
-            const size_t want = (size_t)most * (kThreads / 32);
-            C2A_CUDA(cudaMalloc(&ctx->d_fronts, want * (size_t)C2A_FRONT_CAP * sizeof(Pending)));
-            ctx->fronts_warps = want;
-        }
+        st = ensure_fronts(ctx, (size_t)blocks * (kThreads / 32), (size_t)most * (kThreads / 32));
+        if (st) return st;
         C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
         c2a_canonical_kernel<<<blocks, kThreads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
                                                         d_results, d_contacts, ctx->d_counter, ctx->d_fronts);
@@ -735,6 +762,45 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
                                                        d_results, d_contacts, ctx->d_counter);
     ctx->launches++;
     C2A_CUDA(cudaGetLastError());
+    return C2A_OK;
+}
+
+c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, c2a_distance_result *results)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || (n > 0 && (!queries || !results))) return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    c2a_status st = sync_models(ctx);
+    if (st) return st;
+    const size_t nq = (size_t)n;
+    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
+    const size_t qbytes = up(sizeof(c2a_query) * nq), rbytes = up(sizeof(c2a_distance_result) * nq);
+    st = ensure_buf(ctx, qbytes + rbytes);
+    if (st) return st;
+    c2a_query *dq = (c2a_query *)ctx->d_buf;
+    c2a_distance_result *dr = (c2a_distance_result *)((char *)ctx->d_buf + qbytes);
+    C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    if (!ctx->distance_blocks_per_sm) {
+        int occ = 0;
+        C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_distance_kernel, kThreads, 0));
+        ctx->distance_blocks_per_sm = occ > 0 ? occ : 1;
+    }
+    const int most = ctx->sm_count * ctx->distance_blocks_per_sm;
+    const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
+    const int blocks = need < most ? need : most;
+    st = ensure_fronts(ctx, (size_t)blocks * (kThreads / 32), (size_t)most * (kThreads / 32));
+    if (st) return st;
+    C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), ctx->stream));
+    c2a_distance_kernel<<<blocks, kThreads, 0, ctx->stream>>>(dq, n, ctx->d_models, (int)ctx->models.size(), dr,
+                                                               ctx->d_counter, ctx->d_fronts);
+    ctx->launches++;
+    C2A_CUDA(cudaGetLastError());
+    C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_distance_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int32_t i = 0; i < n; i++)
+        if (results[i].status) return C2A_ERR_QUERY_FAILED;
     return C2A_OK;
 }
 

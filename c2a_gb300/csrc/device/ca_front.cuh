@@ -526,6 +526,57 @@ C2A_KDEV int warp_contacts(Query &q, const M3 &Rroot, V3 Troot, double threshold
 
 /* the C2A_Solve body of the CANONICAL composition on one warp; lane 0 writes
  * the result */
+/* C2A_Distance with rel_err = abs_err = 0 (C2A/src/C2A_PQP.cpp:970-1056) for one
+ * pair: model a at pose[0..11], model b at pose[24..35], seeded with the
+ * query's triangle pair */
+C2A_KDEV void distance_query_warp(const c2a_query &in, const DevModel *models, int num_models,
+                                  c2a_distance_result &out_g, Pending *stack, int cap, int lane)
+{
+    c2a_distance_result out;
+    memset(&out, 0, sizeof(out));
+    const bool bad_models = in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 ||
+                            in.model_b >= num_models || !(models[in.model_a].flags & C2A_MODEL_LIVE) ||
+                            !(models[in.model_b].flags & C2A_MODEL_LIVE);
+    if (bad_models || in.seed_a < 0 || in.seed_a >= models[in.model_a].num_tris || in.seed_b < 0 ||
+        in.seed_b >= models[in.model_b].num_tris) {
+        out.status = C2A_QUERY_BAD_INPUT;
+        if (lane == 0) out_g = out;
+        return;
+    }
+    Query q;
+#ifdef C2A_STATS
+    for (int i = 0; i < ST_COUNT; i++) q.st[i] = 0;
+#endif
+    q.status = 0;
+    q.A = models + in.model_a;
+    q.B = models + in.model_b;
+    q.e_ok = true;
+    q.nbv = q.ntri = 0;
+    const double *P = in.pose;
+    const M3 R1 = pose_R(P), R2 = pose_R(P + 24);
+    const V3 T1 = pose_T(P), T2 = pose_T(P + 24);
+    M3 R;
+    V3 T;
+    relative_transforms(q, R1, T1, R2, T2, R, T); /* res->R, res->T and the root pair (C2A_PQP.cpp:990-1033) */
+    q.shadows_ok = q.e_ok && ((q.A->flags & q.B->flags) & C2A_MODEL_SHADOW_OK);
+    V3 p, qq;
+    TriFeat f;
+    bool col = false;
+    double best = tri_distance_x(q, in.seed_a, in.seed_b, p, qq, f, col);
+    int ba = in.seed_a, bb = in.seed_b;
+    warp_distance(q, R, T, stack, cap, lane, best, ba, bb);
+    tri_distance_x(q, ba, bb, p, qq, f, col); /* the closest pair's points, as its TriDistance left them */
+    out.distance = best;
+    out.p1[0] = p.x; out.p1[1] = p.y; out.p1[2] = p.z;
+    const V3 u = qq - q.Tm; /* res->p2 back into model b's frame (C2A_PQP.cpp:1046-1048) */
+    const V3 p2 = tmul(q.Rm, u);
+    out.p2[0] = p2.x; out.p2[1] = p2.y; out.p2[2] = p2.z;
+    out.tri_a = ba;
+    out.tri_b = bb;
+    out.status = q.status;
+    if (lane == 0) out_g = out;
+}
+
 C2A_KDEV void solve_query_canonical(const c2a_query &in, const DevModel *models, int num_models,
                                     const c2a_params &prm, c2a_result &out_g, c2a_contact *contacts, Pending *stack,
                                     int cap, int lane, int query_index)

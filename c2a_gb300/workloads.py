@@ -219,6 +219,146 @@ def config2(n: int = 65536, seed: int = 2, device: str | None = None, subset: in
     return Workload("config2_torusknot40000_65536q", [knot], qint, poses, default_params(knot.bbox_diag(), 1e-4, 64))
 
 
+def pool_mesh(kind: int, tris: int, seed: int) -> Mesh:
+    """One mesh of the uneven pool: kind 0 a torus knot ((2,3) or (3,5)), 1 a
+    noisy icosphere (sigma 0.02; 20 * 4^k triangles, the k closest to ``tris``
+    in log scale, 3 <= k <= 6), 2 a clustered soup (edge length lognormal
+    mu = -4, sigma = 0.5 of the diagonal)."""
+    if kind == 0:
+        pq = (2, 3) if seed % 2 == 0 else (3, 5)
+        around = max(6, int(round(np.sqrt(tris / 16.0))))
+        segments = max(24, int(round(tris / (2.0 * around))))
+        return torus_knot(pq[0], pq[1], segments, around, 1.0, 0.15 if pq == (2, 3) else 0.1)
+    if kind == 1:
+        k = int(np.clip(np.round(np.log(tris / 20.0) / np.log(4.0)), 3, 6))
+        return icosphere(k, radius=1.0, noise=0.02, seed=seed)
+    return triangle_soup(int(tris), clusters=8, diag=2.0, mu=-4.0, sigma=0.5, seed=seed)
+
+
+def config3(n: int = 4096, seed: int = 3, pool: int = 12, tri_range=(1000, 200000), device: str | None = None,
+            subset: int | None = None) -> Workload:
+    """The uneven batch: ``n`` pairs drawn from a seeded pool of ``pool`` meshes
+    (torus knots, noisy icospheres, clustered soups in turn), triangle counts
+    log-uniform in ``tri_range``; |v| log-uniform in [0.01, 5] diag so CA
+    iteration counts span 1 to the cap; gap U[0.05, 1] diag, |w| U[0, pi];
+    th_ca = 1e-3 of the pool's median diagonal, qsize 64."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]), pool))
+    ms = [pool_mesh(k % 3, counts[k], seed * 1000 + k) for k in range(pool)]
+    pa = rng.integers(0, pool, n)
+    pb = rng.integers(0, pool, n)
+    seeds = rng.integers(0, 2**31 - 1, n)
+    m = n if subset is None else min(subset, n)
+    qint = np.zeros((m, 4), dtype=np.int32)
+    poses = np.zeros((m, POSE_WIDTH))
+    order = np.lexsort((pb[:m], pa[:m]))
+    i = 0
+    while i < m:  # one placement batch per (a, b) combination
+        a, b = pa[order[i]], pb[order[i]]
+        j = i
+        while j < m and pa[order[j]] == a and pb[order[j]] == b:
+            j += 1
+        idx = order[i:j]
+        q, p = ccd_queries(ms[a], ms[b], len(idx), int(seeds[idx[0]]), speed_range=(0.01, 5.0), speed_log=True,
+                           cone_deg=CONFIG2_CONE_DEG, device=device, model_a=int(a), model_b=int(b))
+        qint[idx] = q
+        poses[idx] = p
+        i = j
+    diag = float(np.median([x.bbox_diag() for x in ms]))
+    return Workload(f"config3_pool{pool}_{m}q", ms, qint, poses, default_params(diag, 1e-3, 64))
+
+
+def near_contact_queries(mesh: Mesh, n: int, seed: int, distance_fn, gap_range=(1e-6, 1e-3), tangent_deg=5.0,
+                         speed_range=(0.5, 3.0), max_rot: float = 0.05 * np.pi, device: str | None = None,
+                         model: int = 0) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """``n`` grazing queries of ``mesh`` against itself: B starts at an exact
+    surface gap log-uniform in ``gap_range`` * diag and moves within
+    ``tangent_deg`` of the tangent plane at its closest point (towards or away
+    from A), turning by at most ``max_rot``.
+
+    distance_fn(qint, poses) -> (distance, p1, p2) is an exact distance query
+    (C2A_Distance, rel = abs = 0) for A at pose[0:12] and B at pose[24:36];
+    the skeleton placement is refined along the approach direction by
+    bisection on it.  Returns (qint, poses, achieved gaps)."""
+    rng = np.random.default_rng(seed)
+    diag = mesh.bbox_diag()
+    R0b = random_rotations(rng, n)
+    u = unit_vectors(rng, n)
+    gap = np.exp(rng.uniform(np.log(gap_range[0]), np.log(gap_range[1]), n)) * diag
+    speed = rng.uniform(speed_range[0], speed_range[1], n) * diag
+    tang = unit_vectors(rng, n)
+    phi = np.deg2rad(rng.uniform(-tangent_deg, tangent_deg, n))
+    axis = unit_vectors(rng, n)
+    ang = rng.uniform(0.0, max_rot, n)
+    T0 = place_at_gap(mesh, mesh, R0b, u, np.maximum(gap, 1e-3 * diag), device=device)
+    qint = np.zeros((n, 4), dtype=np.int32)
+    qint[:, 0] = qint[:, 1] = model
+    eye = np.eye(3).reshape(9)
+
+    def poses_at(T):
+        P = np.zeros((n, POSE_WIDTH))
+        P[:, 0:9] = eye
+        P[:, 12:21] = eye
+        P[:, 24:33] = R0b.reshape(n, 9)
+        P[:, 33:36] = T
+        P[:, 36:45] = R0b.reshape(n, 9)
+        P[:, 45:48] = T
+        return P
+
+    def dist(D):
+        d, _, _ = distance_fn(qint, poses_at(T0 + u * D[:, None]))
+        return d
+
+    # bracket the target gap along u (the skeleton estimate is good to ~1e-3 diag), then bisect
+    lo = np.full(n, -4e-3 * diag)
+    hi = np.full(n, 4e-3 * diag)
+    for _ in range(6):
+        dl, dh = dist(lo), dist(hi)
+        lo = np.where(dl >= gap, lo * 2.0, lo)
+        hi = np.where(dh <= gap, hi * 2.0, hi)
+    for _ in range(48):
+        mid = 0.5 * (lo + hi)
+        below = dist(mid) <= gap
+        lo = np.where(below, mid, lo)
+        hi = np.where(below, hi, mid)
+    T = T0 + u * hi[:, None]
+    d, p1, p2 = distance_fn(qint, poses_at(T))
+    q2 = np.einsum("nij,nj->ni", R0b, p2) + T  # B's closest point in A's frame
+    nrm = q2 - p1
+    nn = np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(nn > 0, nrm / np.where(nn > 0, nn, 1.0), u)
+    t = tang - np.sum(tang * nrm, axis=1, keepdims=True) * nrm
+    t /= np.linalg.norm(t, axis=1, keepdims=True)
+    vdir = np.cos(phi)[:, None] * t - np.sin(phi)[:, None] * nrm  # phi > 0: towards A
+    poses = poses_at(T)
+    poses[:, 45:48] = T + speed[:, None] * vdir
+    poses[:, 36:45] = np.einsum("nij,njk->nik", R0b, axis_angle(axis, ang)).reshape(n, 9)
+    return qint, poses, d
+
+
+def gpu_distance_fn(ctx, mesh_id: int):
+    """distance_fn for near_contact_queries through the library's batch distance query."""
+    def fn(qint, poses):
+        q = qint.copy()
+        q[:, 0] = q[:, 1] = mesh_id
+        r = ctx.distance(q, poses)
+        return r["distance"].copy(), r["p1"].copy(), r["p2"].copy()
+    return fn
+
+
+def config4(distance_fn, n: int = 65536, n_near: int = 16384, seed: int = 4, device: str | None = None,
+            subset: int | None = None, near_subset: int | None = None) -> Workload:
+    """Config 2's knots and queries plus ``n_near`` near-contact grazing
+    queries (initial gap log-uniform in [1e-6, 1e-3] diag, velocity within 5
+    degrees of the tangent plane)."""
+    base = config2(n=n, seed=2, device=device, subset=subset)
+    knot = base.meshes[0]
+    m = n_near if near_subset is None else min(near_subset, n_near)
+    qn, pn, _ = near_contact_queries(knot, m, seed, distance_fn, device=device)
+    return Workload(f"config4_torusknot40000_{base.n}q+{m}near", [knot], np.concatenate([base.qint, qn]),
+                    np.concatenate([base.poses, pn]), dict(base.params))
+
+
 def small_knots(n: int, seed: int, segments: int = 24, around: int = 6, device: str | None = None) -> Workload:
     """A quick-to-check variant of config 1 (288-triangle knots) for unit tests."""
     knot = torus_knot(2, 3, segments, around, 1.0, 0.15)

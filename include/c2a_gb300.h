@@ -138,6 +138,20 @@ typedef struct c2a_contact {
     double distance;
 } c2a_contact;
 
+/* Result of one distance query (C2A_Distance with rel_err = abs_err = 0,
+ * C2A/src/C2A_PQP.cpp:970-1056): the exact minimum TriDist over all triangle
+ * pairs.  distance is order-independent; ties between pairs go to the
+ * smallest (tri_a, tri_b), where the reference keeps the first pair its
+ * depth-first order meets. */
+typedef struct c2a_distance_result {
+    double distance;       /* res->distance */
+    double p1[3];          /* closest point on model a, in model a's frame (res->p1) */
+    double p2[3];          /* closest point on model b, in model b's frame (res->p2) */
+    int32_t tri_a, tri_b;  /* the closest pair, post-build indices (the models' last_tri) */
+    int32_t status;        /* C2A_QUERY_* flags */
+    int32_t pad;
+} c2a_distance_result;
+
 /* ---- context --------------------------------------------------------- */
 /* device >= 0: a CUDA device; device == -1: a host-only context that builds
  * and downloads models but runs no query (C2A_ERR_NO_DEVICE). */
@@ -220,6 +234,14 @@ c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, in
 /* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]
  * angular speed, out[4:7] linear velocity, out[7:11] begin quaternion
  * (x, y, z, w). */
+/* C2A_Distance(res, R1, T1, o1, R2, T2, o2, 0, 0, qsize) (C2A/src/C2A_PQP.cpp:970-1056)
+ * for n pairs at once (host buffers; the call synchronises): query i places
+ * model_a by pose[0..11] and model_b by pose[24..35] (the end poses are not
+ * read); seed_a/seed_b give the first upper bound, as o1->last_tri and
+ * o2->last_tri do.  One warp per pair walks a front of node pairs culled by
+ * certified FP32 RSS bounds against the running minimum. */
+c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, c2a_distance_result *results);
+
 c2a_status c2a_motion_setup(const double *R0, const double *T0, const double *R1, const double *T1, double *out);
 /* Pose at time t (clamped to <= 1): R (9), T (3), qua (7: w, x, y, z, T). */
 c2a_status c2a_motion_integrate(const double *R0, const double *T0, const double *R1, const double *T1,

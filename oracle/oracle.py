@@ -89,6 +89,9 @@ class Port:
         L.c2a_port_contact_only.argtypes = [C.POINTER(_PortModel), C.POINTER(_PortModel)] + [C.c_void_p] * 4 + \
                                            [C.c_double, C.c_void_p, C.c_int]
         L.c2a_port_contact_only.restype = C.c_int
+        L.c2a_port_distance.argtypes = [C.POINTER(_PortModel), C.POINTER(_PortModel), C.c_void_p, C.c_void_p,
+                                        C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.c2a_port_distance.restype = C.c_double
 
     def models(self, meshes) -> C.Array:
         """Builds every mesh's hierarchy; returns a ctypes array of models."""
@@ -121,6 +124,16 @@ class Port:
         if bad:
             raise RuntimeError(f"{bad} queries rejected by the oracle port")
         return res, con.reshape(n, max(contacts_per_query, 1))
+
+    def distance(self, models, ia: int, ib: int, R, T, seed_a: int, seed_b: int):
+        """C2A_Distance (rel_err = abs_err = 0) with B placed in A's frame by (R, T):
+        (distance, tri_a, tri_b) in the reference's order and tie rule."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(9)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(3)
+        t = np.zeros(2, dtype=np.int32)
+        d = self.lib.c2a_port_distance(C.byref(models[ia]), C.byref(models[ib]), _dptr(R), _dptr(T), int(seed_a),
+                                       int(seed_b), _dptr(t[0:1]), _dptr(t[1:2]), None, None)
+        return d, int(t[0]), int(t[1])
 
     def rectdist(self, Rab, Tab, a, b):
         Rab = np.ascontiguousarray(Rab, dtype=np.float64).reshape(9)
@@ -163,6 +176,8 @@ class Ref:
         L.c2a_ref_tridist.argtypes = [C.c_void_p] * 9
         L.c2a_ref_tridist.restype = C.c_double
         L.c2a_ref_motion.argtypes = [C.c_void_p] * 4 + [C.c_double] + [C.c_void_p] * 3
+        L.c2a_ref_distance.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_int] + [C.c_void_p] * 4
+        L.c2a_ref_distance.restype = C.c_double
 
     @staticmethod
     def available() -> bool:
@@ -220,6 +235,16 @@ class Ref:
         d = self.lib.c2a_ref_tridist(_dptr(P), _dptr(Q), _dptr(S9), _dptr(T9), _dptr(i[0:1]), _dptr(i[1:2]),
                                      _dptr(i[2:3]), _dptr(i[3:4]), _dptr(i[4:5]))
         return d, P, Q, tuple(int(x) for x in i)
+
+    def distance(self, ha, hb, R, T, seed_a: int, seed_b: int):
+        """The reference's C2A_Distance (rel_err = abs_err = 0, qsize 2): (distance, tri_a, tri_b).
+        ha and hb must be distinct model objects (the query sets each one's last_tri)."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(9)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(3)
+        t = np.zeros(2, dtype=np.int32)
+        d = self.lib.c2a_ref_distance(ha, hb, _dptr(R), _dptr(T), int(seed_a), int(seed_b), _dptr(t[0:1]),
+                                      _dptr(t[1:2]), None, None)
+        return d, int(t[0]), int(t[1])
 
     def motion(self, R0, T0, R1, T1, t):
         args = [np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (R0, T0, R1, T1)]

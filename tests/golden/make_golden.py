@@ -223,11 +223,49 @@ def canonical_fixtures(ref):
     save_workload("canonical_mixed_ref.npz", wl2, *run_ref(ref, hs, wl2, handles_b=hb))
 
 
+def distance_queries(meshes_, pairs, n_per, seed):
+    """Distance-query inputs: for each model pair, random rotations and
+    translations of B (no zero entries, so placing A at the identity leaves
+    R and T unchanged), from overlapping to well apart; random seed pairs."""
+    rng = np.random.default_rng(seed)
+    rows, Rs, Ts = [], [], []
+    for ia, ib in pairs:
+        R = workloads.random_rotations(rng, n_per).reshape(n_per, 9)
+        u = workloads.unit_vectors(rng, n_per)
+        scale = meshes_[ia].bbox_diag() * rng.choice([0.3, 0.7, 1.0, 1.5], n_per) * rng.uniform(0.6, 1.0, n_per)
+        T = u * scale[:, None] + rng.normal(scale=1e-3, size=(n_per, 3))
+        for k in range(n_per):
+            rows.append([ia, ib, rng.integers(meshes_[ia].num_tris), rng.integers(meshes_[ib].num_tris)])
+        Rs.append(R)
+        Ts.append(T)
+    return np.array(rows, dtype=np.int32), np.concatenate(Rs), np.concatenate(Ts)
+
+
+def distance_fixtures(ref):
+    """C2A_Distance (rel_err = abs_err = 0) of the reference on a knot, a soup and an icosphere."""
+    ms = [meshes.torus_knot(2, 3, 100, 16, 1.0, 0.15), meshes.triangle_soup(1000, clusters=6, seed=31),
+          meshes.icosphere(3, radius=0.9, noise=0.02, seed=32)]
+    qint, R, T = distance_queries(ms, [(0, 0), (0, 1), (1, 2), (2, 0), (2, 2)], 24, 301)
+    with quiet_stdout():
+        ha = [ref.model(m) for m in ms]
+        hb = [ref.model(m) for m in ms]
+    out = np.array([ref.distance(ha[a], hb[b], R[i], T[i], sa, sb) for i, (a, b, sa, sb) in enumerate(qint)])
+    arrays = dict(num_meshes=len(ms), qint=qint, R=R, T=T, distance=out[:, 0], tri_a=out[:, 1].astype(np.int32),
+                  tri_b=out[:, 2].astype(np.int32))
+    for i, m in enumerate(ms):
+        arrays[f"mesh{i}_verts"] = m.verts
+        arrays[f"mesh{i}_faces"] = m.faces
+    np.savez_compressed(os.path.join(HERE, "distance_ref.npz"), **arrays)
+
+
 def main():
     build(ref=True)
     ref = Ref()
     if sys.argv[1:] == ["canonical"]:
         canonical_fixtures(ref)
+        return
+    if sys.argv[1:] == ["distance"]:
+        distance_fixtures(ref)
         return
 
     # 1. config-1 mesh (3,200-triangle (2,3) knots), 96 queries of the config-1 family, default seeds
@@ -270,6 +308,7 @@ def main():
     motion_vectors(ref)
     bvh_hashes(ref)
     canonical_fixtures(ref)
+    distance_fixtures(ref)
 
 
 if __name__ == "__main__":
