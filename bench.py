@@ -54,8 +54,12 @@ def parse():
     p.add_argument("--queries", type=int, default=65536)
     p.add_argument("--cpu-sample", type=int, default=0, help="queries in the CPU-baseline sample (0: auto)")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--mode", choices=["reference", "canonical"], default="reference",
-                   help="reference: the reference's results bit for bit; canonical: closest-pair-seeded steps")
+    p.add_argument("--mode", choices=["reference", "canonical", "learned"], default="reference",
+                   help="reference: the reference's results bit for bit; canonical: closest-pair-seeded steps; "
+                        "learned: train the seeding network on the uneven pool, then hinted vs plain "
+                        "CANONICAL batches on held-out queries")
+    p.add_argument("--train", type=int, default=262144, help="--mode learned: training queries")
+    p.add_argument("--epochs", type=int, default=6, help="--mode learned: training epochs")
     p.add_argument("--engine", choices=["auto", "warp", "thread", "batched"], default="auto")
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
@@ -202,14 +206,50 @@ def config_dict(wl, args, sample_only=None):
             "triangles_per_model": wl.meshes[0].num_tris, "models": "two (2,3) torus-knot tubes, 400 x 50",
             "th_ca": wl.params["th_ca"], "t_delta": wl.params["tol_t"], "qsize": wl.params["qsize"],
             "mode": args.mode, "engine": args.engine, "traversal": traversal,
-            "seeding": "plain (triangle 0 of each model, as after EndModel); no learned seeding (not built)",
+            "seeding": "plain (triangle 0 of each model, as after EndModel); the learned seeding is measured "
+                       "by --mode learned (CANONICAL mode only: REFERENCE results depend on the seed)",
             "contacts_per_query": CONTACT_SLOTS, "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": f"replicas x{args.gpus}"}
+
+
+def run_learned(args, rank, world, local):
+    """The learned seeding on the uneven pool (config 3's mesh pool): labels
+    from the exact distance query, training on the library's own kernels,
+    then held-out CANONICAL batches, plain and hinted, each timed once."""
+    import torch
+    from c2a_gb300 import api, build, learned
+
+    torch.cuda.set_device(local)
+    if rank == 0:
+        build.build()
+    if rank != 0:
+        return
+    t0 = time.time()
+    r = learned.experiment(n_train=args.train, n_eval=args.queries, epochs=args.epochs, pool=12,
+                           tri_range=(1000, 200000), engine=api.ENGINE_BATCHED, seed=3,
+                           log=lambda m: print(m, file=sys.stderr, flush=True))
+    line = {"metric": METRIC, "value": r["hinted_qps"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": r["hinted_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 CA / bf16 network", "impl": "learned",
+            "data": "synthetic: seeded config-3 mesh pool (torus knots, noisy icospheres, clustered soups)",
+            "config": {"workload": f"config3 pool of 12 meshes ({min(r['pool_tris'])}-{max(r['pool_tris'])} "
+                                   f"triangles), {args.queries} held-out queries", "mode": "canonical",
+                       "engine": "batched", "train_queries": args.train, "epochs": args.epochs,
+                       "network": "50->256->256->256->4096, GELU, bf16 weights, fp32 accumulation", "top_k": 8},
+            "plain_qps": r["plain_qps"], "speedup_vs_plain": r["speedup"], "identical_results": r["identical"],
+            "differing_fields": r["differ"], "true_pair_hint_qps": args.queries / r["oracle_hint_ms"] * 1e3,
+            "top1": r["top1"], "top8": r["topk"], "train_loss": r["loss"], "label_s": r["label_s"],
+            "train_s": r["train_s"], "wall_s": time.time() - t0, "colliding": r["colliding"],
+            "e2e": None, "roofline": None, "cpu_baseline": None, "gpu_launches": None}
+    print(json.dumps(line), flush=True)
 
 
 def main():
     args = parse()
     rank, world, local = env_rank()
+    if args.mode == "learned" and args.impl == "ours":
+        run_learned(args, rank, world, local)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

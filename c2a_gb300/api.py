@@ -40,7 +40,7 @@ QUERY_BAD_INPUT, QUERY_STACK_OVERFLOW, QUERY_CONTACT_OVERFLOW, QUERY_ITER_CAP = 
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
                "c2a_model_info", "c2a_model_download", "c2a_model_free", "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
-               "c2a_distance_batch",
+               "c2a_distance_batch", "c2a_solve_batch_hinted",
                "c2a_motion_setup", "c2a_motion_integrate"]
 
 

@@ -386,7 +386,8 @@ __global__ void __launch_bounds__(kThreads) c2a_canonical_kernel(const c2a_query
                                                                  c2a_result *__restrict__ results,
                                                                  c2a_contact *__restrict__ contacts,
                                                                  unsigned int *__restrict__ counter,
-                                                                 Pending *__restrict__ fronts)
+                                                                 Pending *__restrict__ fronts,
+                                                                 const uint32_t *__restrict__ hints, int nh)
 {
     const int lane = threadIdx.x & 31;
     const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -398,7 +399,7 @@ __global__ void __launch_bounds__(kThreads) c2a_canonical_kernel(const c2a_query
         if (q >= (unsigned int)n) break;
         c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
         solve_query_canonical(queries[q], models, num_models, prm, results[q], cq, stack, C2A_FRONT_CAP, lane,
-                              (int)q);
+                              (int)q, hints ? hints + (size_t)q * nh * 2 : nullptr, nh);
     }
 }
 
@@ -692,8 +693,30 @@ c2a_status c2a_model_free(c2a_context *ctx, int32_t id)
     return C2A_OK;
 }
 
+namespace {
+c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
+                        c2a_result *d_results, c2a_contact *d_contacts, void *stream, const uint32_t *hints, int nh);
+}
+
 c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
                                   c2a_result *d_results, c2a_contact *d_contacts, void *stream)
+{
+    return solve_device(ctx, d_queries, n, params, d_results, d_contacts, stream, nullptr, 0);
+}
+
+c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
+                                  const uint32_t *d_hints, int32_t hints_per_query, c2a_result *d_results,
+                                  c2a_contact *d_contacts, void *stream)
+{
+    if (!params || params->mode != C2A_MODE_CANONICAL || hints_per_query < 0 || hints_per_query > 16 ||
+        (hints_per_query > 0 && !d_hints))
+        return C2A_ERR_INVALID_ARGUMENT;
+    return solve_device(ctx, d_queries, n, params, d_results, d_contacts, stream, d_hints, hints_per_query);
+}
+
+namespace {
+c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
+                        c2a_result *d_results, c2a_contact *d_contacts, void *stream, const uint32_t *hints, int nh)
 {
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
@@ -708,7 +731,7 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
     if (!d_contacts) prm.contacts_per_query = 0;
     if (prm.mode == C2A_MODE_CANONICAL && prm.engine == C2A_ENGINE_BATCHED)
         return wave_solve(&ctx->wave, ctx->sm_count, s, d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
-                          d_results, d_contacts, &ctx->launches);
+                          d_results, d_contacts, &ctx->launches, hints, nh);
     if (prm.mode == C2A_MODE_CANONICAL) {
         if (!ctx->canonical_blocks_per_sm) {
             int occ = 0;
@@ -722,7 +745,8 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
         if (st) return st;
         C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
         c2a_canonical_kernel<<<blocks, kThreads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
-                                                        d_results, d_contacts, ctx->d_counter, ctx->d_fronts);
+                                                        d_results, d_contacts, ctx->d_counter, ctx->d_fronts, hints,
+                                                        nh);
         ctx->launches++;
         C2A_CUDA(cudaGetLastError());
         return C2A_OK;
@@ -764,6 +788,7 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
     C2A_CUDA(cudaGetLastError());
     return C2A_OK;
 }
+} // namespace
 
 c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, c2a_distance_result *results)
 {

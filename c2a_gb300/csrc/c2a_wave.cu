@@ -159,17 +159,6 @@ C2A_KDEV double dmargin(const Query &q)
 
 C2A_KDEV float ru_float(double x) { return __double2float_ru(x); }
 
-/* squared distance between the rectangle centres of a child pair, B's
- * rectangle placed by (R, T) in A's frame (a descent heuristic only) */
-C2A_KDEV double centre_dist2(const Query &q, const M3 &R, V3 T, int x1, int x2)
-{
-    const NodeRec *n1 = q.A->nodes + x1, *n2 = q.B->nodes + x2;
-    const V3 ca = v3(0.5 * __ldg(&n1->l[0]), 0.5 * __ldg(&n1->l[1]), 0.0);
-    const V3 cb = mul(R, v3(0.5 * __ldg(&n2->l[0]), 0.5 * __ldg(&n2->l[1]), 0.0)) + T;
-    const V3 d = cb - ca;
-    return dot(d, d);
-}
-
 /* warp-aggregated append of n (0..2) entries to a list (any set of active
  * lanes); returns the first index, or -1 when the list is full (the overflow
  * flag is raised) */
@@ -270,7 +259,8 @@ __global__ void __launch_bounds__(kWThreads) k_init(const c2a_query *__restrict_
 /* transforms, the seed's exact distance, a greedy descent, the root item */
 __global__ void __launch_bounds__(kWThreads) k_step_begin(const int32_t *__restrict__ active, int na,
                                                           Query *__restrict__ qs, WLoop *__restrict__ loops,
-                                                          WAcc *__restrict__ acc, Lists L, int out)
+                                                          WAcc *__restrict__ acc, Lists L, int out,
+                                                          const uint32_t *__restrict__ hints, int nh)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     int push = 0;
@@ -287,48 +277,13 @@ __global__ void __launch_bounds__(kWThreads) k_step_begin(const int32_t *__restr
         TriFeat f;
         bool col = false;
         double best = tri_distance_x(q, q.seed_a, q.seed_b, p, qq, f, col);
-        /* greedy descent: the child pair with the smaller lower bound */
-        int b1 = 0, b2 = 0;
-        M3 Rc = R;
-        V3 Tc = T;
-        for (int depth = 0; depth < 4 * C2A_STACK_DEPTH; depth++) {
-            int fc1, fc2;
-            if (is_leaf_pair(q, b1, b2, fc1, fc2)) {
-                const double d = tri_distance_x(q, -fc1 - 1, -fc2 - 1, p, qq, f, col);
-                if (d < best) best = d;
-                break;
-            }
-            int side, a1, a2, c1, c2;
-            child_pairs(q, b1, b2, fc1, fc2, side, a1, a2, c1, c2);
-            float la, lc;
-            EFCtx ec{false};
-            const M3T<EF> Re = ef_m3(Rc, ec);
-            const V3T<EF> Te = ef_v3(Tc, ec);
-            if (q.shadows_ok && !ec.bad) {
-                la = bv_lower(q, side, Re, Te, a1, a2);
-                lc = bv_lower(q, side, Re, Te, c1, c2);
-            } else {
-                la = bv_lower_exact(q, side, Rc, Tc, a1, a2);
-                lc = bv_lower_exact(q, side, Rc, Tc, c1, c2);
-            }
-            /* the smaller lower bound; while both RSS pairs overlap, the closer centres */
-            M3 Ra, Rcc;
-            V3 Ta, Tcc;
-            child_transform(q, side, a1, a2, Rc, Tc, Ra, Ta);
-            child_transform(q, side, c1, c2, Rc, Tc, Rcc, Tcc);
-            bool take_c = lc < la;
-            if (lc == la) take_c = centre_dist2(q, Rcc, Tcc, c1, c2) < centre_dist2(q, Ra, Ta, a1, a2);
-            if (take_c) {
-                b1 = c1;
-                b2 = c2;
-                Rc = Rcc;
-                Tc = Tcc;
-            } else {
-                b1 = a1;
-                b2 = a2;
-                Rc = Ra;
-                Tc = Ta;
-            }
+        /* a greedy descent and, at the first step, the hinted descents tighten the bound */
+        const int use = (q.numCA == 0 && hints) ? nh : 0;
+        for (int h = -1; h < use; h++) {
+            int ta, tb;
+            const double d = descend_to_leaf(q, R, T, h < 0 ? 0u : hints[(size_t)qi * nh * 2 + 2 * h],
+                                             h < 0 ? 0u : hints[(size_t)qi * nh * 2 + 2 * h + 1], ta, tb);
+            if (ta >= 0 && d < best) best = d;
         }
         WAcc &a = acc[qi];
         a.best_bits = (unsigned long long)__double_as_longlong(best);
@@ -1227,7 +1182,7 @@ c2a_status set_counter(WaveBuffers *b, cudaStream_t s, int which, int32_t v)
 /* one full batch; returns C2A_OK, an error, or (overflow) C2A_ERR_OUT_OF_MEMORY with *overflow set */
 c2a_status run_batch(WaveBuffers *b, cudaStream_t s, const c2a_query *d_queries, int n, const DevModel *d_models,
                      int num_models, const c2a_params &prm, c2a_result *d_results, c2a_contact *d_contacts,
-                     int64_t *launches, bool *overflow)
+                     int64_t *launches, bool *overflow, const uint32_t *hints, int nh)
 {
     Lists &L = b->L;
     *overflow = false;
@@ -1254,7 +1209,8 @@ c2a_status run_batch(WaveBuffers *b, cudaStream_t s, const c2a_query *d_queries,
         if (st) return st;
         int cur = 0;
         if (trace_on()) fprintf(stderr, "step: %d active\n", na);
-        k_step_begin<<<grid1(na), kWThreads, 0, s>>>(L.active[cur_active], na, b->qs, b->loops, b->acc, L, cur);
+        k_step_begin<<<grid1(na), kWThreads, 0, s>>>(L.active[cur_active], na, b->qs, b->loops, b->acc, L, cur,
+                                                     hints, nh);
         st = set_counter(b, s, 7, 0);
         if (st) return st;
         k_dsearch<<<b->search_warps / (kWThreads / 32), kWThreads, 0, s>>>(L.active[cur_active], na, b->qs, b->acc,
@@ -1387,7 +1343,7 @@ c2a_status run_batch(WaveBuffers *b, cudaStream_t s, const c2a_query *d_queries,
 
 c2a_status wave_solve(WaveBuffers **bufs, int sm_count, cudaStream_t s, const c2a_query *d_queries, int n,
                       const DevModel *d_models, int num_models, const c2a_params &prm, c2a_result *d_results,
-                      c2a_contact *d_contacts, int64_t *launches)
+                      c2a_contact *d_contacts, int64_t *launches, const uint32_t *hints, int nh)
 {
     if (!*bufs) {
         WaveBuffers *b = new (std::nothrow) WaveBuffers();
@@ -1410,7 +1366,7 @@ c2a_status wave_solve(WaveBuffers **bufs, int sm_count, cudaStream_t s, const c2
         }
         bool overflow = false;
         const c2a_status st = run_batch(b, s, d_queries, n, d_models, num_models, prm, d_results, d_contacts,
-                                        launches, &overflow);
+                                        launches, &overflow, hints, nh);
         if (!overflow) return st;
         /* a list ran out of room: grow every list and solve the batch again */
         C2A_WCUDA(cudaStreamSynchronize(s));

@@ -168,6 +168,131 @@ C2A_KDEV void own_transform(const Query &q, const Pending &e, M3 &R, V3 &T)
     }
 }
 
+/* ------------------------------------------------------- seed descents */
+
+/* a hinted node: its path from the root in the low 16 bits (bit k: which
+ * child, 0 first_child, 1 first_child + 1, at depth k) and its depth above */
+C2A_KDEV int hint_depth(uint32_t h) { return (int)(h >> 16); }
+
+/* squared distance between the rectangle centres of a child pair, B's
+ * rectangle placed by (R, T) in A's frame (a descent heuristic only) */
+C2A_KDEV double rect_centre_dist2(const Query &q, const M3 &R, V3 T, int x1, int x2)
+{
+    const NodeRec *n1 = q.A->nodes + x1, *n2 = q.B->nodes + x2;
+    const V3 ca = v3(0.5 * __ldg(&n1->l[0]), 0.5 * __ldg(&n1->l[1]), 0.0);
+    const V3 cb = mul(R, v3(0.5 * __ldg(&n2->l[0]), 0.5 * __ldg(&n2->l[1]), 0.0)) + T;
+    const V3 d = cb - ca;
+    return dot(d, d);
+}
+
+/* one descent from the root pair (placed by R, T) to a leaf pair: while the
+ * model being split is above its hinted node (ha for A, hb for B; depth 0:
+ * no hint) it follows the hint's path, otherwise the child pair with the
+ * smaller certified lower bound is taken (while both RSS pairs overlap, the
+ * one with the closer rectangle centres).  Returns the leaf pair's exact
+ * distance (C2A_TriDistance) and its triangles in ta, tb; an upper bound of
+ * the closest-pair distance, so any descent may seed the search. */
+C2A_KDEV double descend_to_leaf(const Query &q, const M3 &Rroot, V3 Troot, uint32_t ha, uint32_t hb, int &ta,
+                                int &tb)
+{
+    int b1 = 0, b2 = 0, da = 0, db = 0;
+    M3 Rc = Rroot;
+    V3 Tc = Troot;
+    for (int step = 0; step < 4 * C2A_STACK_DEPTH; step++) {
+        const int fc1 = __ldg(&q.A->nodes[b1].first_child), fc2 = __ldg(&q.B->nodes[b2].first_child);
+        if (fc1 < 0 && fc2 < 0) {
+            ta = -fc1 - 1;
+            tb = -fc2 - 1;
+            V3 p, qq;
+            TriFeat f;
+            bool col = false;
+            return tri_distance_x(q, ta, tb, p, qq, f, col);
+        }
+        int side, a1, a2, c1, c2;
+        child_pairs(q, b1, b2, fc1, fc2, side, a1, a2, c1, c2);
+        const int dpt = side == 0 ? da : db;
+        const uint32_t h = side == 0 ? ha : hb;
+        M3 Ra, Rcc;
+        V3 Ta, Tcc;
+        child_transform(q, side, a1, a2, Rc, Tc, Ra, Ta);
+        child_transform(q, side, c1, c2, Rc, Tc, Rcc, Tcc);
+        bool take_c;
+        if (dpt < hint_depth(h)) {
+            take_c = ((h >> dpt) & 1u) != 0;
+        } else {
+            float la, lc;
+            EFCtx ec{false};
+            const M3T<EF> Re = ef_m3(Rc, ec);
+            const V3T<EF> Te = ef_v3(Tc, ec);
+            if (q.shadows_ok && !ec.bad) {
+                la = bv_lower(q, side, Re, Te, a1, a2);
+                lc = bv_lower(q, side, Re, Te, c1, c2);
+            } else {
+                la = bv_lower_exact(q, side, Rc, Tc, a1, a2);
+                lc = bv_lower_exact(q, side, Rc, Tc, c1, c2);
+            }
+            take_c = lc < la;
+            if (lc == la) take_c = rect_centre_dist2(q, Rcc, Tcc, c1, c2) < rect_centre_dist2(q, Ra, Ta, a1, a2);
+        }
+        if (side == 0) da++;
+        else db++;
+        if (take_c) {
+            b1 = c1;
+            b2 = c2;
+            Rc = Rcc;
+            Tc = Tcc;
+        } else {
+            b1 = a1;
+            b2 = a2;
+            Rc = Ra;
+            Tc = Ta;
+        }
+    }
+    ta = tb = -1;
+    return __longlong_as_double(0x7ff0000000000000LL);
+}
+
+/* the warp's smallest (d, a, b), exact ties to the smallest pair */
+C2A_KDEV void warp_min_pair(double &d, int &a, int &b)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double d2 = __shfl_xor_sync(kFullMask, d, o);
+        const int a2 = __shfl_xor_sync(kFullMask, a, o), b2 = __shfl_xor_sync(kFullMask, b, o);
+        if (d2 < d || (d2 == d && (a2 < a || (a2 == a && b2 < b)))) {
+            d = d2;
+            a = a2;
+            b = b2;
+        }
+    }
+}
+
+/* the seed of a closest-pair search: (best, ba, bb) becomes the smallest of
+ * itself and the descents run on lanes 0..nd-1 (lane 0 greedy, lane l > 0
+ * towards hinted pair l - 1), keeping distance and pair together */
+C2A_KDEV void seed_descents(const Query &q, const M3 &R, V3 T, const uint32_t *hints, int nd, int lane,
+                            double &best, int &ba, int &bb)
+{
+    double dl = __longlong_as_double(0x7ff0000000000000LL);
+    int la = 0x7fffffff, lb = 0x7fffffff;
+    if (lane < nd) {
+        int ta = -1, tb = -1;
+        const double d = descend_to_leaf(q, R, T, lane ? hints[2 * (lane - 1)] : 0u,
+                                         lane ? hints[2 * (lane - 1) + 1] : 0u, ta, tb);
+        if (ta >= 0) {
+            dl = d;
+            la = ta;
+            lb = tb;
+        }
+    }
+    warp_min_pair(dl, la, lb);
+    if (dl < best || (dl == best && (la < ba || (la == ba && lb < bb)))) {
+        best = dl;
+        ba = la;
+        bb = lb;
+    }
+}
+
 C2A_KDEV Pending root_entry(const M3 &R, V3 T)
 {
     Pending r;
@@ -377,9 +502,12 @@ C2A_KDEV void warp_traverse(Query &q, const M3 &Rroot, V3 Troot, Pending *stack,
 
 /* ------------------------------------------------------------ one step */
 
-/* C2A_Distance, then C2A_TimeOfContactStep seeded with the closest pair */
+/* C2A_Distance, then C2A_TimeOfContactStep seeded with the closest pair.
+ * The search's first bound is the seed pair's distance, tightened by a
+ * greedy descent (lane 0) and, at the first step, by descents towards the
+ * hinted cluster pairs (lanes 1..nh); none of these changes the result. */
 C2A_KDEV void canonical_step(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, bool translation, Pending *stack, int cap,
-                             int lane)
+                             int lane, const uint32_t *hints = nullptr, int nh = 0)
 {
     if (translation) { /* the reference's translation step, one private stack per lane */
         toc_step(q, R1, T1, R2, T2, true, stack + lane * C2A_STACK_DEPTH);
@@ -398,6 +526,7 @@ C2A_KDEV void canonical_step(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, bool tran
         best = tri_distance_x(q, q.seed_a, q.seed_b, p, qq, f, col);
     }
     int ba = q.seed_a, bb = q.seed_b;
+    seed_descents(q, R, T, hints, 1 + ((q.numCA == 0 && hints) ? nh : 0), lane, best, ba, bb);
     warp_distance(q, R, T, stack, cap, lane, best, ba, bb);
     if (q.status) return;
     q.seed_a = ba;
@@ -564,6 +693,7 @@ C2A_KDEV void distance_query_warp(const c2a_query &in, const DevModel *models, i
     bool col = false;
     double best = tri_distance_x(q, in.seed_a, in.seed_b, p, qq, f, col);
     int ba = in.seed_a, bb = in.seed_b;
+    seed_descents(q, R, T, nullptr, 1, lane, best, ba, bb); /* a greedy descent may tighten the first bound */
     warp_distance(q, R, T, stack, cap, lane, best, ba, bb);
     tri_distance_x(q, ba, bb, p, qq, f, col); /* the closest pair's points, as its TriDistance left them */
     out.distance = best;
@@ -579,7 +709,8 @@ C2A_KDEV void distance_query_warp(const c2a_query &in, const DevModel *models, i
 
 C2A_KDEV void solve_query_canonical(const c2a_query &in, const DevModel *models, int num_models,
                                     const c2a_params &prm, c2a_result &out_g, c2a_contact *contacts, Pending *stack,
-                                    int cap, int lane, int query_index)
+                                    int cap, int lane, int query_index, const uint32_t *hints = nullptr,
+                                    int nh = 0)
 {
     c2a_result out;
     memset(&out, 0, sizeof(out));
@@ -623,7 +754,7 @@ C2A_KDEV void solve_query_canonical(const c2a_query &in, const DevModel *models,
 
     double toc = 0, lamda = 0.0, lastLamda = 0, dlamda = 0.0;
     bool collisionfree = false;
-    canonical_step(q, R1, T1, R2, T2, translation, stack, cap, lane);
+    canonical_step(q, R1, T1, R2, T2, translation, stack, cap, lane, hints, nh);
     double dist = q.distance, mint = q.mint;
     if (translation) {
         collisionfree = (mint >= 1.0);

@@ -1,0 +1,430 @@
+/*
+ * mlp.cu -- the learned seeding's network kernels (include/c2a_mlp.h).
+ *
+ * GEMM: out = A B^T with A (M x K) and B (N x K) in bf16, K contiguous, on
+ * the tensor cores (mma.sync m16n8k16, bf16 in, FP32 accumulate).  A block
+ * computes a 128 x 128 tile with eight warps (2 x 4, 64 x 32 each); K moves
+ * in steps of 32 through a double-buffered shared-memory stage filled with
+ * 16-byte cp.async copies, fragments come from ldmatrix.  Rows are padded to
+ * 80 bytes so that the eight row addresses of an ldmatrix hit eight different
+ * 16-byte bank groups.  The epilogue adds the bias and applies GELU (erff,
+ * called) in registers and writes FP32 and/or bf16.
+ *
+ * Everything else (transposes, GELU backward, softmax cross-entropy, column
+ * sums, Adam, the input assembly and its embedding scatter, top-k) is
+ * bandwidth-bound elementwise or row-wise work.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/c2a_mlp.h"
+
+namespace {
+
+c2a_status launch_status()
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return C2A_OK;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return C2A_ERR_NO_DEVICE;
+    return C2A_ERR_CUDA;
+}
+
+__device__ __forceinline__ float bf2f(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
+__device__ __forceinline__ uint16_t f2bf(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x)
+{
+    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+    return cdf + x * pdf;
+}
+
+/* ------------------------------------------------------------------ GEMM */
+
+constexpr int kBM = 128, kBN = 128, kBK = 32;
+constexpr int kRowH = kBK + 8; /* bf16 per shared-memory row (80 bytes) */
+constexpr int kGemmThreads = 256;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t r[4], const void *smem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(s));
+}
+
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+                 "{%8, %9}, {%0, %1, %2, %3};\n"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+/* one K-step of the A and B tiles into stage buffers (each thread: two 16-byte
+ * chunks of A, two of B; a tile row is 32 bf16 = four chunks) */
+__device__ __forceinline__ void load_stage(const uint16_t *A, const uint16_t *B, int K, int m0, int n0, int k0,
+                                           uint16_t *sA, uint16_t *sB)
+{
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const int c = threadIdx.x + i * kGemmThreads; /* 0..511 */
+        const int row = c >> 2, col = (c & 3) * 8;
+        cp_async16(sA + row * kRowH + col, A + (size_t)(m0 + row) * K + k0 + col);
+        cp_async16(sB + row * kRowH + col, B + (size_t)(n0 + row) * K + k0 + col);
+    }
+}
+
+__global__ void __launch_bounds__(kGemmThreads) k_gemm(const uint16_t *__restrict__ A, const uint16_t *__restrict__ B,
+                                                       const float *__restrict__ bias, int M, int N, int K,
+                                                       int flags, float *__restrict__ out_f32,
+                                                       uint16_t *__restrict__ out_bf16)
+{
+    __shared__ __align__(16) uint16_t sA[2][kBM * kRowH];
+    __shared__ __align__(16) uint16_t sB[2][kBN * kRowH];
+    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32; /* this warp's 64 x 32 sub-tile */
+    float acc[4][4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.0f;
+
+    const int steps = K / kBK;
+    load_stage(A, B, K, m0, n0, 0, sA[0], sB[0]);
+    cp_async_commit();
+    for (int s = 0; s < steps; s++) {
+        const int cur = s & 1;
+        if (s + 1 < steps) {
+            load_stage(A, B, K, m0, n0, (s + 1) * kBK, sA[cur ^ 1], sB[cur ^ 1]);
+            cp_async_commit();
+            cp_async_wait1();
+        } else {
+            cp_async_wait0();
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < kBK; kk += 16) {
+            uint32_t af[4][4], bfr[2][4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) { /* A rows wm + 16 i .. + 15, k kk .. kk + 15 */
+                const int r = wm + 16 * i + (lane & 15), c = kk + (lane >> 4) * 8;
+                ldmatrix_x4(af[i], sA[cur] + r * kRowH + c);
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++) { /* B rows (n) wn + 16 j .. + 15 */
+                const int r = wn + 16 * j + (lane & 7) + ((lane >> 4) << 3), c = kk + ((lane >> 3) & 1) * 8;
+                ldmatrix_x4(bfr[j], sB[cur] + r * kRowH + c);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j >> 1][(j & 1) * 2], bfr[j >> 1][(j & 1) * 2 + 1]);
+        }
+        __syncthreads();
+    }
+    /* epilogue: c0, c1 at (row g, cols 2 t, 2 t + 1), c2, c3 at row g + 8 */
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int row = m0 + wm + 16 * i + g + 8 * h, col = n0 + wn + 8 * j + 2 * t;
+                float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
+                if (flags & C2A_MLP_BIAS) {
+                    v0 += bias[col];
+                    v1 += bias[col + 1];
+                }
+                const size_t o = (size_t)row * N + col;
+                if (out_f32) *reinterpret_cast<float2 *>(out_f32 + o) = make_float2(v0, v1);
+                if (out_bf16) {
+                    if (flags & C2A_MLP_GELU) {
+                        v0 = gelu(v0);
+                        v1 = gelu(v1);
+                    }
+                    *reinterpret_cast<uint32_t *>(out_bf16 + o) = (uint32_t)f2bf(v0) | ((uint32_t)f2bf(v1) << 16);
+                }
+            }
+}
+
+/* ------------------------------------------------------ elementwise/rows */
+
+__global__ void k_transpose(const uint16_t *__restrict__ in, int rows, int cols, uint16_t *__restrict__ out)
+{
+    __shared__ uint16_t tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += 8) tile[i][threadIdx.x] = in[(size_t)(r0 + i) * cols + c0 + threadIdx.x];
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += 8) out[(size_t)(c0 + i) * rows + r0 + threadIdx.x] = tile[threadIdx.x][i];
+}
+
+__global__ void k_gelu_backward(const float *__restrict__ d_act, const float *__restrict__ pre, int64_t count,
+                                uint16_t *__restrict__ d_pre)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        d_pre[i] = f2bf(d_act[i] * gelu_grad(pre[i]));
+}
+
+__device__ __forceinline__ float block_reduce(float v, float *sh, bool is_max)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        const float w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = is_max ? fmaxf(v, w) : v + w;
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    v = lane < nw ? sh[lane] : (is_max ? -INFINITY : 0.0f);
+    for (int o = 16; o > 0; o >>= 1) {
+        const float w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = is_max ? fmaxf(v, w) : v + w;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_softmax_xent(const float *__restrict__ logits, const int32_t *__restrict__ labels,
+                                                      int N, float scale, float *__restrict__ loss,
+                                                      uint16_t *__restrict__ d_logits)
+{
+    __shared__ float sh[32];
+    const int m = blockIdx.x;
+    const float *x = logits + (size_t)m * N;
+    uint16_t *d = d_logits + (size_t)m * N;
+    const int lab = labels[m];
+    if (lab < 0 || lab >= N) {
+        for (int n = threadIdx.x; n < N; n += blockDim.x) d[n] = 0;
+        if (threadIdx.x == 0) loss[m] = 0.0f;
+        return;
+    }
+    float mx = -INFINITY;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) mx = fmaxf(mx, x[n]);
+    mx = block_reduce(mx, sh, true);
+    float s = 0.0f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) s += expf(x[n] - mx);
+    s = block_reduce(s, sh, false);
+    const float inv = 1.0f / s;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        const float p = expf(x[n] - mx) * inv;
+        d[n] = f2bf((p - (n == lab ? 1.0f : 0.0f)) * scale);
+    }
+    if (threadIdx.x == 0) loss[m] = logf(s) + mx - x[lab];
+}
+
+/* column sums: block = 32 columns x 8 row groups */
+__global__ void k_colsum(const uint16_t *__restrict__ in, int M, int N, float *__restrict__ out)
+{
+    __shared__ float sh[8][33];
+    const int col = blockIdx.x * 32 + threadIdx.x;
+    float s = 0.0f;
+    if (col < N)
+        for (int m = threadIdx.y; m < M; m += 8) s += bf2f(in[(size_t)m * N + col]);
+    sh[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && col < N) {
+        float t = 0.0f;
+        for (int i = 0; i < 8; i++) t += sh[i][threadIdx.x];
+        out[col] = t;
+    }
+}
+
+__global__ void k_adam(float *__restrict__ w, float *__restrict__ m, float *__restrict__ v, const float *__restrict__ g,
+                       int64_t count, float lr, float b1, float b2, float eps, float c1, float c2,
+                       uint16_t *__restrict__ wb, uint16_t *__restrict__ wbt, int rows, int cols)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.0f - b1) * gi;
+        const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[i] = wi;
+        const uint16_t h = f2bf(wi);
+        if (wb) wb[i] = h;
+        if (wbt) {
+            const int64_t r = i / cols, c = i - r * cols;
+            wbt[c * rows + r] = h;
+        }
+    }
+}
+
+__global__ void k_assemble(const float *__restrict__ feat, const int32_t *__restrict__ ia,
+                           const int32_t *__restrict__ ib, const float *__restrict__ emb, int n_valid, int M, int K,
+                           uint16_t *__restrict__ x)
+{
+    const int64_t total = (int64_t)M * K;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = (int)(i / K), k = (int)(i - (int64_t)m * K);
+        float v = 0.0f;
+        if (m < n_valid) {
+            if (k < 18) v = feat[(size_t)m * 18 + k];
+            else if (k < 34) v = emb[(size_t)ia[m] * 16 + (k - 18)];
+            else if (k < 50) v = emb[(size_t)ib[m] * 16 + (k - 34)];
+        }
+        x[i] = f2bf(v);
+    }
+}
+
+__global__ void k_embed_backward(const float *__restrict__ dx, const int32_t *__restrict__ ia,
+                                 const int32_t *__restrict__ ib, int n_valid, int K, float *__restrict__ g_emb)
+{
+    const int64_t total = (int64_t)n_valid * 32;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int m = (int)(i >> 5), k = (int)(i & 31);
+        const float d = dx[(size_t)m * K + 18 + k];
+        if (k < 16) atomicAdd(g_emb + (size_t)ia[m] * 16 + k, d);
+        else atomicAdd(g_emb + (size_t)ib[m] * 16 + (k - 16), d);
+    }
+}
+
+/* top-k of a row on one warp: each lane keeps its k best (value desc, index
+ * asc), then k rounds of a warp arg-max over the lanes' heads */
+__global__ void k_topk(const float *__restrict__ logits, int M, int N, int k, int32_t *__restrict__ index)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= M) return;
+    const float *x = logits + (size_t)warp * N;
+    float bv[16];
+    int bi[16];
+    for (int i = 0; i < 16; i++) {
+        bv[i] = -INFINITY;
+        bi[i] = 0x7fffffff;
+    }
+    for (int n = lane; n < N; n += 32) {
+        float v = x[n];
+        int id = n;
+        for (int i = 0; i < k; i++) { /* insertion into the descending list */
+            const bool better = v > bv[i] || (v == bv[i] && id < bi[i]);
+            if (better) {
+                const float tv = bv[i];
+                const int ti = bi[i];
+                bv[i] = v;
+                bi[i] = id;
+                v = tv;
+                id = ti;
+            }
+        }
+    }
+    int head = 0;
+    for (int r = 0; r < k; r++) {
+        float v = head < k ? bv[head] : -INFINITY;
+        int id = head < k ? bi[head] : 0x7fffffff;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float v2 = __shfl_xor_sync(0xffffffffu, v, o);
+            const int i2 = __shfl_xor_sync(0xffffffffu, id, o);
+            if (v2 > v || (v2 == v && i2 < id)) {
+                v = v2;
+                id = i2;
+            }
+        }
+        if (lane == 0) index[(size_t)warp * k + r] = id;
+        if (head < k && bi[head] == id) head++;
+    }
+}
+
+int grid_for(int64_t count, int threads)
+{
+    int64_t b = (count + threads - 1) / threads;
+    return (int)(b < 152 * 32 ? (b > 0 ? b : 1) : 152 * 32);
+}
+
+} // namespace
+
+extern "C" {
+
+c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias, int32_t M, int32_t N, int32_t K,
+                        int32_t flags, float *out_f32, uint16_t *out_bf16, void *stream)
+{
+    if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % kBM || N % kBN || K % kBK || ((flags & C2A_MLP_BIAS) && !bias))
+        return C2A_ERR_INVALID_ARGUMENT;
+    const dim3 grid(N / kBN, M / kBM);
+    k_gemm<<<grid, kGemmThreads, 0, (cudaStream_t)stream>>>(A, B, bias, M, N, K, flags, out_f32, out_bf16);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_transpose(const uint16_t *in, int32_t rows, int32_t cols, uint16_t *out, void *stream)
+{
+    if (!in || !out || rows <= 0 || cols <= 0 || rows % 32 || cols % 32) return C2A_ERR_INVALID_ARGUMENT;
+    k_transpose<<<dim3(cols / 32, rows / 32), dim3(32, 8), 0, (cudaStream_t)stream>>>(in, rows, cols, out);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_gelu_backward(const float *d_act, const float *pre, int64_t count, uint16_t *d_pre, void *stream)
+{
+    if (!d_act || !pre || !d_pre || count <= 0) return C2A_ERR_INVALID_ARGUMENT;
+    k_gelu_backward<<<grid_for(count, 256), 256, 0, (cudaStream_t)stream>>>(d_act, pre, count, d_pre);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_softmax_xent(const float *logits, const int32_t *labels, int32_t M, int32_t N, float scale,
+                                float *loss, uint16_t *d_logits, void *stream)
+{
+    if (!logits || !labels || !loss || !d_logits || M <= 0 || N <= 0) return C2A_ERR_INVALID_ARGUMENT;
+    k_softmax_xent<<<M, 256, 0, (cudaStream_t)stream>>>(logits, labels, N, scale, loss, d_logits);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_colsum(const uint16_t *in, int32_t M, int32_t N, float *out, void *stream)
+{
+    if (!in || !out || M <= 0 || N <= 0) return C2A_ERR_INVALID_ARGUMENT;
+    k_colsum<<<(N + 31) / 32, dim3(32, 8), 0, (cudaStream_t)stream>>>(in, M, N, out);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_adam(float *w, float *m, float *v, const float *g, int64_t count, float lr, float beta1,
+                        float beta2, float eps, int32_t t, uint16_t *w_bf16, uint16_t *w_bf16_t, int32_t rows,
+                        int32_t cols, void *stream)
+{
+    if (!w || !m || !v || !g || count <= 0 || t < 1 || (w_bf16_t && (int64_t)rows * cols != count))
+        return C2A_ERR_INVALID_ARGUMENT;
+    const float c1 = 1.0f - powf(beta1, (float)t), c2 = 1.0f - powf(beta2, (float)t);
+    k_adam<<<grid_for(count, 256), 256, 0, (cudaStream_t)stream>>>(w, m, v, g, count, lr, beta1, beta2, eps, c1, c2,
+                                                                    w_bf16, w_bf16_t, rows, cols);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_assemble(const float *feat, const int32_t *ia, const int32_t *ib, const float *emb,
+                            int32_t n_valid, int32_t M, int32_t K, uint16_t *x, void *stream)
+{
+    if (!feat || !ia || !ib || !emb || !x || K < 50 || K % 32 || n_valid < 0 || n_valid > M || M <= 0)
+        return C2A_ERR_INVALID_ARGUMENT;
+    k_assemble<<<grid_for((int64_t)M * K, 256), 256, 0, (cudaStream_t)stream>>>(feat, ia, ib, emb, n_valid, M, K, x);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_embed_backward(const float *dx, const int32_t *ia, const int32_t *ib, int32_t n_valid, int32_t K,
+                                  float *g_emb, void *stream)
+{
+    if (!dx || !ia || !ib || !g_emb || K < 50 || n_valid < 0) return C2A_ERR_INVALID_ARGUMENT;
+    if (n_valid == 0) return C2A_OK;
+    k_embed_backward<<<grid_for((int64_t)n_valid * 32, 256), 256, 0, (cudaStream_t)stream>>>(dx, ia, ib, n_valid, K,
+                                                                                             g_emb);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_topk(const float *logits, int32_t M, int32_t N, int32_t k, int32_t *index, void *stream)
+{
+    if (!logits || !index || M <= 0 || N <= 0 || k < 1 || k > 16 || k > N) return C2A_ERR_INVALID_ARGUMENT;
+    k_topk<<<(M * 32 + 255) / 256, 256, 0, (cudaStream_t)stream>>>(logits, M, N, k, index);
+    return launch_status();
+}
+
+} // extern "C"

@@ -25,10 +25,12 @@ struct WaveBuffers;
 
 /* solves d_queries[0, n) into d_results (contacts in fixed slots of
  * prm.contacts_per_query); synchronises the stream between waves.  bufs is
- * created on first use and reused; *launches counts kernel launches. */
+ * created on first use and reused; *launches counts kernel launches.
+ * hints (device, nh pairs of hinted nodes per query, may be NULL) seed the
+ * first step's search bound. */
 c2a_status wave_solve(WaveBuffers **bufs, int sm_count, cudaStream_t s, const c2a_query *d_queries, int n,
                       const DevModel *d_models, int num_models, const c2a_params &prm, c2a_result *d_results,
-                      c2a_contact *d_contacts, int64_t *launches);
+                      c2a_contact *d_contacts, int64_t *launches, const uint32_t *hints = nullptr, int nh = 0);
 
 void wave_free(WaveBuffers *bufs);
 

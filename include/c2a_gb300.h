@@ -234,6 +234,19 @@ c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, in
 /* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]
  * angular speed, out[4:7] linear velocity, out[7:11] begin quaternion
  * (x, y, z, w). */
+/* c2a_solve_batch_device in C2A_MODE_CANONICAL with hints: d_hints holds, per
+ * query, hints_per_query (<= 16) pairs of hinted BVH nodes (model a's, then
+ * model b's), each encoded as its path from the root in the low 16 bits (bit
+ * k: the child taken at depth k, 0 first_child, 1 first_child + 1) and its
+ * depth in the high 16 bits.  At the first CA step, a descent towards each
+ * hinted pair gives an exact triangle-pair distance that may tighten the
+ * closest-pair search's first bound.  Results are those of the unhinted
+ * call, bit for bit (the search is exact); only its pruning changes.  The
+ * learned seeding (c2a_gb300/learned.py) produces these hints. */
+c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
+                                  const uint32_t *d_hints, int32_t hints_per_query, c2a_result *d_results,
+                                  c2a_contact *d_contacts, void *stream);
+
 /* C2A_Distance(res, R1, T1, o1, R2, T2, o2, 0, 0, qsize) (C2A/src/C2A_PQP.cpp:970-1056)
  * for n pairs at once (host buffers; the call synchronises): query i places
  * model_a by pose[0..11] and model_b by pose[24..35] (the end poses are not

@@ -12,20 +12,24 @@ from c2a_testutil import GOLDEN, bits
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "c2a_gb300.h")).read()
+def declared_symbols(header="c2a_gb300.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(c2a_[a-z_0-9]+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_symbol(lib):
-    from c2a_gb300 import api
+    from c2a_gb300 import api, learned
 
     names = declared_symbols()
     assert len(names) >= 14
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     assert sorted(api.ABI_SYMBOLS) == names
+    mlp = declared_symbols("c2a_mlp.h")
+    assert [n for n in mlp if not hasattr(lib, n)] == []
+    assert sorted(learned.MLP_SYMBOLS) == mlp
+    learned.bind(lib)  # every signature binds
 
 
 def test_status_strings_and_host_only_context(lib):
