@@ -237,7 +237,8 @@ def run_learned(args, rank, world, local):
                        "engine": "batched", "train_queries": args.train, "epochs": args.epochs,
                        "network": "50->256->256->256->4096, GELU, bf16 weights, fp32 accumulation", "top_k": 8},
             "plain_qps": r["plain_qps"], "speedup_vs_plain": r["speedup"], "identical_results": r["identical"],
-            "differing_fields": r["differ"], "true_pair_hint_qps": args.queries / r["oracle_hint_ms"] * 1e3,
+            "differing_fields": r["differ"], "contact_overflow_queries": r["contact_overflow_queries"],
+            "true_pair_hint_qps": args.queries / r["oracle_hint_ms"] * 1e3,
             "top1": r["top1"], "top8": r["topk"], "train_loss": r["loss"], "label_s": r["label_s"],
             "train_s": r["train_s"], "wall_s": time.time() - t0, "colliding": r["colliding"],
             "e2e": None, "roofline": None, "cpu_baseline": None, "gpu_launches": None}

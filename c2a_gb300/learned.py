@@ -460,10 +460,13 @@ def experiment(n_train: int = 2_000_000, n_eval: int = 65536, epochs: int = 4, p
         used = np.minimum(rp["num_contact"], cpq)
         cfields = ("type_a", "type_b", "fid_a", "fid_b", "tri_a", "tri_b", "pa", "pb", "distance")
         for i in range(n_eval):
+            if rp["num_contact"][i] > cpq:
+                continue  # more contacts than slots: which ones are stored is unspecified in CANONICAL mode
             a, b = cp[i * cpq:i * cpq + used[i]], ch[i * cpq:i * cpq + used[i]]
             differ += [f"contact.{f}" for f in cfields if a[f].tobytes() != b[f].tobytes()]
         out["differ"] = sorted(set(differ))
         same = same_c = not differ
+        out["contact_overflow_queries"] = int(np.sum(rp["num_contact"] > cpq))
         out.update(plain_ms=ms_plain, hinted_ms=ms_hint, plain_qps=n_eval / ms_plain * 1e3,
                    hinted_qps=n_eval / ms_hint * 1e3, speedup=ms_plain / ms_hint, identical=bool(same and same_c),
                    colliding=float(np.mean(rp["collisionfree"] == 0)),

@@ -91,7 +91,9 @@ typedef struct c2a_params {
  * result is independent of traversal order; one warp runs each query over a
  * parallel front.  Results equal that composition of the reference's own
  * functions; contacts come sorted by (tri_a, tri_b), seed_a/seed_b are the
- * last step's closest pair (ties: the smallest pair). */
+ * last step's closest pair (ties: the smallest pair).  When a query has more
+ * contacts than contacts_per_query, num_contact and C2A_QUERY_CONTACT_OVERFLOW
+ * are exact but which of them fill the slots is unspecified in this mode. */
 #define C2A_MODE_REFERENCE 0
 #define C2A_MODE_CANONICAL 1
 
