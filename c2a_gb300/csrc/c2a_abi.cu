@@ -84,6 +84,8 @@ struct c2a_context {
     size_t order_cap = 0;
     int canonical_blocks_per_sm = 0;
     int warp_blocks_per_sm = 0;
+    int warp_cap = 0;            /* the warp kernel's stack entries the occupancy above was computed for */
+    bool warp_smem_attr = false;
     int distance_blocks_per_sm = 0;
     std::mutex mu;
 };
@@ -164,11 +166,12 @@ bool params_ok(const c2a_params *p)
 }
 
 /* queries must not pair models deeper than the traversal stack */
-c2a_status check_depths(c2a_context *ctx)
+c2a_status check_depths(c2a_context *ctx, int *deepest_out = nullptr)
 {
     int deepest = 0;
     for (const ModelSlot &s : ctx->models)
         if (s.live && s.host.depth > deepest) deepest = s.host.depth;
+    if (deepest_out) *deepest_out = deepest;
     if (2 * deepest + 2 > C2A_STACK_DEPTH) return C2A_ERR_TREE_TOO_DEEP;
     return C2A_OK;
 }
@@ -360,13 +363,14 @@ __global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel
                                                                   c2a_result *__restrict__ results,
                                                                   c2a_contact *__restrict__ contacts,
                                                                   unsigned int *__restrict__ counter,
-                                                                  const int32_t *__restrict__ order)
+                                                                  const int32_t *__restrict__ order, int stack_cap)
 {
-    extern __shared__ unsigned char c2a_warp_smem[];
-    WarpShared *sh = reinterpret_cast<WarpShared *>(c2a_warp_smem);
+    extern __shared__ __align__(16) unsigned char c2a_warp_smem[];
     Pending tstack[C2A_STACK_DEPTH]; /* the translation-only step's sequential stack */
     const int lane = threadIdx.x & 31;
-    WarpShared &mine = sh[threadIdx.x >> 5];
+    WarpShared &mine = *reinterpret_cast<WarpShared *>(c2a_warp_smem + (threadIdx.x >> 5) *
+                                                       warp_shared_bytes(stack_cap));
+    mine.cap = stack_cap;
     for (;;) {
         unsigned int q = 0;
         if (lane == 0) q = atomicAdd(counter, 1u);
@@ -722,7 +726,8 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
     if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
     if (n == 0) return C2A_OK;
     C2A_CUDA(cudaSetDevice(ctx->device));
-    c2a_status st = check_depths(ctx);
+    int deepest = 0;
+    c2a_status st = check_depths(ctx, &deepest);
     if (st) return st;
     st = sync_models(ctx);
     if (st) return st;
@@ -753,13 +758,19 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
     }
     C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
     if (prm.engine != C2A_ENGINE_THREAD) {
-        const size_t smem = sizeof(WarpShared) * (kThreads / 32);
-        if (!ctx->warp_blocks_per_sm) {
+        /* the stack holds one pending pair per BVTT level: 2 depth + 2 entries */
+        const int cap = 2 * deepest + 2 > 4 ? 2 * deepest + 2 : 4;
+        const size_t smem = warp_shared_bytes(cap) * (kThreads / 32);
+        if (!ctx->warp_smem_attr) {
             C2A_CUDA(cudaFuncSetAttribute(c2a_solve_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
+                                          (int)(warp_shared_bytes(C2A_STACK_DEPTH) * (kThreads / 32))));
+            ctx->warp_smem_attr = true;
+        }
+        if (ctx->warp_cap != cap) {
             int occ = 0;
             C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_solve_warp_kernel, kThreads, smem));
             ctx->warp_blocks_per_sm = occ > 0 ? occ : 1;
+            ctx->warp_cap = cap;
         }
         const int most = ctx->sm_count * ctx->warp_blocks_per_sm;
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
@@ -776,7 +787,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
                                                              ctx->d_order, ctx->d_counter + 1);
         c2a_solve_warp_kernel<<<need < most ? need : most, kThreads, smem, s>>>(
             d_queries, n, ctx->d_models, (int)ctx->models.size(), prm, d_results, d_contacts, ctx->d_counter,
-            ctx->d_order);
+            ctx->d_order, cap);
         ctx->launches += 2;
         C2A_CUDA(cudaGetLastError());
         return C2A_OK;

@@ -49,12 +49,24 @@ struct WStackEntry {
     V3 T;
 };
 
-/* per-warp shared state */
+/* per-warp shared state: the query (one copy per warp; every lane computes
+ * the same values, so every lane may write them), the children of the pair
+ * just expanded, each half's RectDist slots (rect_table.cuh), then the stack
+ * of pending second children, `cap` entries (set at launch from the deepest
+ * hierarchy in the context) */
 struct WarpShared {
-    WStackEntry stack[C2A_STACK_DEPTH];
-    WStackEntry child[2]; /* the children of the pair just expanded */
-    double rt[2][64];     /* each half's RectDist slots (rect_table.cuh) */
+    Query q;
+    WStackEntry child[2];
+    double rt[2][64];
+    int32_t cap, pad_[3];
+    WStackEntry stack[1]; /* cap entries */
 };
+
+/* bytes of one warp's shared state with a stack of cap entries (16-byte multiple) */
+__host__ __device__ constexpr size_t warp_shared_bytes(int cap)
+{
+    return ((offsetof(WarpShared, stack) + (size_t)cap * sizeof(WStackEntry)) + 15) / 16 * 16;
+}
 
 C2A_KDEV double shfl_d(double v, int src) { return __shfl_sync(kWFull, v, src); }
 C2A_KDEV V3 shfl_v3(V3 v, int src) { return v3(shfl_d(v.x, src), shfl_d(v.y, src), shfl_d(v.z, src)); }
@@ -421,7 +433,7 @@ C2A_KDEV void child_test_x(const Query &q, int x1, int x2, const M3 &R, V3 T, do
     load_x(n2, q.B->nodes + x2);
     V3 S = v3(0, 0, 0);
     C2A_WCLOCK(xc0);
-    double z = rect_dist_half(R, T, n1.l, n2.l, S, q.rt, lane);
+    double z = rect_dist_half(R, T, n1.l, n2.l, S, q.rt + 64 * (lane >> 4), lane);
     C2A_WCLOCK(xc1);
     C2A_WSTAT(q, ST_W_CYC_X_RECT, xc1 - xc0);
     z -= (n1.r + n2.r);
@@ -662,14 +674,14 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
             C2A_WCLOCK(l1);
             C2A_WSTAT(q, ST_W_CYC_LEAF, l1 - l0);
         } else {
-            if (sp >= C2A_STACK_DEPTH) {
+            if (sp >= sh.cap) {
                 q.status |= C2A_QUERY_STACK_OVERFLOW;
                 return;
             }
             expand_warp(q, b1, b2, fc1, fc2, R, T, sh, lane);
             C2A_WCLOCK(k0);
             q.nbv += 2;
-            WStackEntry a = sh.child[0], c = sh.child[1];
+            WStackEntry &a = sh.child[0], &c = sh.child[1];
             const bool c_first = closer_second_w(q, a, c, lane);
             WStackEntry &first = c_first ? c : a;
             if (lane == 0) sh.stack[sp] = c_first ? a : c;
@@ -689,7 +701,7 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
         }
         C2A_WCLOCK(p0);
         while (!go && sp > 0) {
-            WStackEntry e = sh.stack[--sp];
+            WStackEntry &e = sh.stack[--sp];
             if (descend_w(q, e, lane)) {
                 b1 = e.b1;
                 b2 = e.b2;
@@ -808,12 +820,12 @@ C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double thresh
                 count++;
             }
         } else {
-            if (sp >= C2A_STACK_DEPTH) {
+            if (sp >= sh.cap) {
                 q.status |= C2A_QUERY_STACK_OVERFLOW;
                 return count;
             }
             expand_warp(q, b1, b2, fc1, fc2, R, T, sh, lane);
-            WStackEntry a = sh.child[0], c = sh.child[1];
+            WStackEntry &a = sh.child[0], &c = sh.child[1];
             const bool c_first = closer_second_w(q, a, c, lane);
             WStackEntry &first = c_first ? c : a;
             if (lane == 0) sh.stack[sp] = c_first ? a : c;
@@ -828,7 +840,7 @@ C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double thresh
             __syncwarp();
         }
         while (!go && sp > 0) {
-            WStackEntry e = sh.stack[--sp];
+            WStackEntry &e = sh.stack[--sp];
             if (contact_descend_w(q, e, threshold, lane)) {
                 b1 = e.b1;
                 b2 = e.b2;
@@ -863,7 +875,7 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
         if (lane == 0) out_g = out;
         return;
     }
-    Query q;
+    Query &q = sh.q; /* one copy per warp in shared memory, written with the same values by every lane */
 #ifdef C2A_STATS
     for (int i = 0; i < ST_COUNT; i++) q.st[i] = 0;
     for (int i = 0; i < ST_COUNT - ST_W_FIRST; i++) q.wst[i] = 0;
@@ -873,7 +885,7 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
     q.A = models + in.model_a;
     q.B = models + in.model_b;
     q.want_mint = true;
-    q.rt = sh.rt[lane >> 4];
+    q.rt = &sh.rt[0][0];
     const double *P = in.pose;
     set_motions(q, P);
     q.toc_delta = prm.toc_delta;
