@@ -49,6 +49,9 @@ struct WStackEntry {
     V3 T;
 };
 
+static_assert(sizeof(WStackEntry) % 8 == 0 && offsetof(WStackEntry, T) == offsetof(WStackEntry, R) + sizeof(M3),
+              "a record is copied as 8-byte words and its transform written as 12 contiguous doubles");
+
 /* per-warp shared state: the query (one copy per warp; every lane computes
  * the same values, so every lane may write them), the children of the pair
  * just expanded, each half's RectDist slots (rect_table.cuh), then the stack
@@ -336,8 +339,9 @@ C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const doubl
 {
     const int half = lane >> 4, k = lane & 15;
     __syncwarp(); /* the previous call's reads of V are done */
-    if (k < kRtInputs) V[k] = rt_input(k, R, T, a, b);
-    if (k < kRtStage1) V[kRtInputs + k] = rt_stage1(k, R, T, a, b);
+    rt_inputs(R, T, a, b, V);
+    __syncwarp();
+    if (k < kRtStage1) V[kRtInputs + k] = rt_stage1(k, R, T, V);
     __syncwarp();
 #pragma unroll
     for (int r = 0; r < 3; r++) {
@@ -391,7 +395,7 @@ C2A_KDEV double pick3(double a, double b, double c, int i) { return i == 0 ? a :
  * lanes 9..11 T[k - 9], with the expression trees of tmmul/tmul (side 0) or
  * mmul/mul_add (side 1); the half then shares the twelve values */
 C2A_KDEV void child_transform_lanes(const Query &q, int side, int x1, int x2, const M3 &PR, V3 PT, M3 &R, V3 &T,
-                                    int lane)
+                                    double &own, int lane)
 {
     const int half = lane >> 4, k = lane & 15;
     const NodeRec *n = side == 0 ? q.A->nodes + x1 : q.B->nodes + x2;
@@ -419,6 +423,7 @@ C2A_KDEV void child_transform_lanes(const Query &q, int side, int x1, int x2, co
     }
     double v = a0 * b0 + a1 * b1 + a2 * b2;
     if (side == 1 && isT) v = v + c;
+    own = v; /* lane k < 12 of the half: R.m[k], then T */
     const int base = 16 * half;
 #pragma unroll
     for (int e = 0; e < 9; e++) R.m[e] = shfl_d(v, base + e);
@@ -532,8 +537,9 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
     const int x1 = half ? c1 : a1, x2 = half ? c2 : a2;
     M3 R;
     V3 T;
+    double own;
     C2A_WCLOCK(w0);
-    child_transform_lanes(q, side, x1, x2, PR, PT, R, T, lane);
+    child_transform_lanes(q, side, x1, x2, PR, PT, R, T, own, lane);
     C2A_WCLOCK(w1);
     EF d = ef_exact(0.0f), m = ef_exact(0.0f);
     bool d_zero = false;
@@ -551,8 +557,9 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
     C2A_WSTAT(q, ST_W_CYC_XFORM, w1 - w0);
     C2A_WSTAT(q, ST_W_CYC_TEST_E, w2 - w1);
     C2A_WSTAT(q, ST_W_CYC_TEST_X, w3 - w2);
+    WStackEntry &e = sh.child[half];
+#if C2A_WARP_FILTER
     if ((lane & 15) == 0) {
-        WStackEntry &e = sh.child[half];
         e.b1 = x1;
         e.b2 = x2;
         e.exact = exact;
@@ -570,6 +577,16 @@ C2A_KDEV void expand_warp(const Query &q, int b1, int b2, int fc1, int fc2, cons
         e.R = R;
         e.T = T;
     }
+#else
+    { /* the record written across the half: lane k < 12 its own transform entry */
+        const int k = lane & 15;
+        if (k < 12) reinterpret_cast<double *>(&e.R)[k] = own; /* R then T, contiguous */
+        else if (k == 12) { e.b1 = x1; e.b2 = x2; }
+        else if (k == 13) { e.exact = exact; e.pad = 0; }
+        else if (k == 14) e.d = dx;
+        else e.m = mx;
+    }
+#endif
     __syncwarp();
     C2A_WCLOCK(w4);
     C2A_WSTAT(q, ST_W_CYC_STORE, w4 - w3);
@@ -593,6 +610,9 @@ C2A_KDEV void make_exact_warp(const Query &q, WStackEntry &e, int lane)
 /* mint < UpboundTOC && (d < distance - abs_err || d * (1 + rel_err) < distance) (C2A.cpp:1281-1351) */
 C2A_KDEV bool descend_w(const Query &q, WStackEntry &e, int lane)
 {
+#if !C2A_WARP_FILTER /* every record is exact */
+    return e.m < q.upbound && ((e.d < (q.distance - q.abs_err)) || (e.d * (1 + q.rel_err) < q.distance));
+#endif
     if (q.shadows_ok) {
         const int a = ef_lt3(e.m_e, q.upbound_e);
         const int b = ef_lt3(e.d_e, q.bound_e);
@@ -607,7 +627,7 @@ C2A_KDEV bool descend_w(const Query &q, WStackEntry &e, int lane)
 /* a pruned pair's mint lowers res->mint (C2A.cpp:1290-1311) */
 C2A_KDEV void contribute_w(Query &q, WStackEntry &e, int lane)
 {
-    if (q.shadows_ok && ef_lt3(e.m_e, q.mint_e) == 0) return; /* certainly >= the current minimum */
+    if (C2A_WARP_FILTER && q.shadows_ok && ef_lt3(e.m_e, q.mint_e) == 0) return; /* certainly >= the current minimum */
     make_exact_warp(q, e, lane);
     if (e.m < q.mint) {
         q.mint = e.m;
@@ -618,6 +638,9 @@ C2A_KDEV void contribute_w(Query &q, WStackEntry &e, int lane)
 /* d2 < d1 (C2A.cpp:1281) */
 C2A_KDEV bool closer_second_w(const Query &q, WStackEntry &a, WStackEntry &c, int lane)
 {
+#if !C2A_WARP_FILTER /* every record is exact */
+    return c.d < a.d;
+#endif
     const int r = ef_lt3(c.d_e, a.d_e);
     if (r >= 0 && q.shadows_ok) return r == 1;
     make_exact_warp(q, a, lane);
@@ -684,7 +707,10 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
             WStackEntry &a = sh.child[0], &c = sh.child[1];
             const bool c_first = closer_second_w(q, a, c, lane);
             WStackEntry &first = c_first ? c : a;
-            if (lane == 0) sh.stack[sp] = c_first ? a : c;
+            { /* the pending second child onto the stack, one 8-byte word per lane */
+                const double *src = reinterpret_cast<const double *>(c_first ? &a : &c);
+                if (lane < (int)(sizeof(WStackEntry) / 8)) reinterpret_cast<double *>(&sh.stack[sp])[lane] = src[lane];
+            }
             sp++;
             if (descend_w(q, first, lane)) {
                 b1 = first.b1;
@@ -791,6 +817,9 @@ C2A_KDEV bool contact_leaf_warp(Query &q, int fc1, int fc2, double threshold, in
 /* d < threshold (abs_err = rel_err = 0: both of the reference's clauses) */
 C2A_KDEV bool contact_descend_w(const Query &q, WStackEntry &e, double threshold, int lane)
 {
+#if !C2A_WARP_FILTER /* every record is exact */
+    return (e.d < (threshold - 0)) || (e.d * (1.0 + 0) < threshold);
+#endif
     if (q.shadows_ok) {
         EFCtx tc{false};
         const EF te = in_d(threshold, tc);
@@ -828,7 +857,10 @@ C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double thresh
             WStackEntry &a = sh.child[0], &c = sh.child[1];
             const bool c_first = closer_second_w(q, a, c, lane);
             WStackEntry &first = c_first ? c : a;
-            if (lane == 0) sh.stack[sp] = c_first ? a : c;
+            { /* the pending second child onto the stack, one 8-byte word per lane */
+                const double *src = reinterpret_cast<const double *>(c_first ? &a : &c);
+                if (lane < (int)(sizeof(WStackEntry) / 8)) reinterpret_cast<double *>(&sh.stack[sp])[lane] = src[lane];
+            }
             sp++;
             if (contact_descend_w(q, first, threshold, lane)) {
                 b1 = first.b1;

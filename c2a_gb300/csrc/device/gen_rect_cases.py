@@ -420,13 +420,21 @@ def write_table(pre: str, exprs: dict, rows: list):
     w(f"    return {expr};")
     w("}")
     w("")
-    w("/* lane k's stage-1 slot (k < kRtStage1): a product of two inputs, or Tba.x /")
-    w(" * Tba.y as tmul evaluates them */")
-    w("C2A_DEV double rt_stage1(int k, const M3 &R, V3 T, const double a[2], const double b[2])")
+    w("/* every input slot (all lanes of a half write the same values) */")
+    w("C2A_DEV void rt_inputs(const M3 &R, V3 T, const double a[2], const double b[2], double *V)")
+    w("{")
+    vals2 = ["a[0]", "a[1]", "b[0]", "b[1]", "R.m[0]", "R.m[1]", "R.m[3]", "R.m[4]", "T.x", "T.y", "0.0"]
+    for k, v in enumerate(vals2):
+        w(f"    V[{k}] = {v};")
+    w("}")
+    w("")
+    w("/* lane k's stage-1 slot (k < kRtStage1): a product of two input slots, or")
+    w(" * Tba.x / Tba.y as tmul evaluates them */")
+    w("C2A_DEV double rt_stage1(int k, const M3 &R, V3 T, const double *V)")
     w("{")
     w("    if (k < 8) {")
     w("        const uint32_t w = C2A_RT(rt_s1, k);")
-    w("        return rt_input(w & 0x7f, R, T, a, b) * rt_input((w >> 8) & 0x7f, R, T, a, b);")
+    w("        return V[w & 0x7f] * V[(w >> 8) & 0x7f];")
     w("    }")
     w("    const int c = k - 8; /* column c of R: Tba[c] = R[0][c] T.x + R[1][c] T.y + R[2][c] T.z */")
     w("    return R.m[c] * T.x + R.m[3 + c] * T.y + R.m[6 + c] * T.z;")

@@ -250,8 +250,8 @@ int c2a_fc_rect_table(const double *Rab9, const double *Tab3, const double *a, c
     const M3 R = m3_of(Rab9);
     const V3 T = v3(Tab3[0], Tab3[1], Tab3[2]);
     double V[64];
-    for (int k = 0; k < kRtInputs; k++) V[k] = rt_input(k, R, T, a, b);
-    for (int k = 0; k < kRtStage1; k++) V[kRtInputs + k] = rt_stage1(k, R, T, a, b);
+    rt_inputs(R, T, a, b, V);
+    for (int k = 0; k < kRtStage1; k++) V[kRtInputs + k] = rt_stage1(k, R, T, V);
     for (int i = 0; i < kRtStage2; i++) V[kRtStage2Base + i] = rt_stage2(i, V);
     unsigned mask = 0;
     for (int g = 0; g < 8; g++)
