@@ -341,10 +341,15 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": peak_src, "kernel": KERNELS.get((args.mode, args.engine)),
                 "algorithmic_bytes_per_launch": alg_bytes, "num_bv_tests": bv, "num_tri_tests": tri,
-                "note": "not HBM-bound: the traversal is a dependent chain of FP64 node-pair tests; its binding "
-                        "resource is the FP64 pipe (see fp64_pipe) and, for the heaviest queries, latency"}
+                "note": "not HBM-bound (the trees stay in L2): each query is a dependent chain of FP64 node-pair "
+                        "tests whose correctly rounded divisions and square roots set the latency of an "
+                        "expansion at 8 warps per SM; the batch's makespan is set by its heaviest queries "
+                        "(warp slots busy 63 % of the time) -- see fp64_pipe and profiles/"}
     if prof and prof.get("fp64_pipe_active_pct") is not None:
         roofline["fp64_pipe"] = {"active_pct_of_peak": prof["fp64_pipe_active_pct"],
+                                 "fp64_share_of_instructions": (prof["inst_executed_fp64"] / prof["inst_executed"]
+                                                                if prof.get("inst_executed") else None),
+                                 "warp_slot_utilization_full_batch": prof.get("full_batch_warp_slot_utilization"),
                                  "source": prof.get("source", "profiles")}
 
     e2e = None
