@@ -61,6 +61,10 @@ def parse():
     p.add_argument("--train", type=int, default=262144, help="--mode learned: training queries")
     p.add_argument("--epochs", type=int, default=6, help="--mode learned: training epochs")
     p.add_argument("--engine", choices=["auto", "warp", "thread", "batched"], default="auto")
+    p.add_argument("--order", choices=["learned", "geometric"], default="learned",
+                   help="REFERENCE mode: the work-queue order; learned: a cost model trained on another seed's "
+                        "queries (costs measured by the library) starts the costliest queries first; geometric: "
+                        "queries whose bounding spheres approach first.  Results are identical either way.")
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
 
@@ -208,6 +212,7 @@ def config_dict(wl, args, sample_only=None):
             "mode": args.mode, "engine": args.engine, "traversal": traversal,
             "seeding": "plain (triangle 0 of each model, as after EndModel); the learned seeding is measured "
                        "by --mode learned (CANONICAL mode only: REFERENCE results depend on the seed)",
+            "order": args.order if args.mode == "reference" else "geometric",
             "contacts_per_query": CONTACT_SLOTS, "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -286,9 +291,44 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
 
-    def step():
+    def plain_step():
         ctx.solve_device(d_q.data_ptr(), n, wl.params, d_r.data_ptr(), d_c.data_ptr(), CONTACT_SLOTS,
                          stream=stream.cuda_stream)
+
+    learned_info = None
+    step = plain_step
+    if args.mode == "reference" and args.order == "learned":
+        from c2a_gb300 import learned
+
+        t_setup = time.time()
+        diag = wl.meshes[0].bbox_diag()
+        wl_tr = workloads.config2(n=args.queries, seed=1000 + rank, device=f"cuda:{local}")
+        q_tr = wl_tr.qint.copy()
+        q_tr[:, :2] = mid
+        res_tr, _ = ctx.solve(q_tr, wl_tr.poses, wl.params, contacts_per_query=0)
+        cost_tr = learned.query_cost(res_tr)
+        f_tr = learned.features(wl_tr.poses, np.full(wl_tr.n, diag), np.full(wl_tr.n, diag))
+        cut = (wl_tr.n * 4 // 5) // 1024 * 1024  # 80 % to train on, the rest held out
+        cost_model = learned.CostOrder(1, seed=rank)
+        zeros_tr = np.zeros(wl_tr.n, dtype=np.int32)
+        hist = cost_model.fit(f_tr[:cut], zeros_tr[:cut], zeros_tr[:cut], cost_tr[:cut], epochs=30)
+        held = cost_model.expected(torch.tensor(f_tr[cut:], device="cuda"), torch.tensor(zeros_tr[cut:], device="cuda"),
+                                   torch.tensor(zeros_tr[cut:], device="cuda")).cpu().numpy()
+        rank_r = float(np.corrcoef(np.argsort(np.argsort(held)), np.argsort(np.argsort(cost_tr[cut:])))[0, 1])
+        feat_dev = torch.tensor(learned.features(wl.poses, np.full(n, diag), np.full(n, diag)), device="cuda")
+        zeros_dev = torch.zeros(n, dtype=torch.int32, device="cuda")
+        learned_info = {"train_queries": cut, "held_out_queries": wl_tr.n - cut, "train_seed": 1000 + rank,
+                        "epochs": 30, "final_loss": hist[-1], "held_out_rank_correlation": rank_r,
+                        "used": rank_r >= 0.6, "setup_s": time.time() - t_setup}
+
+        def learned_step():
+            with torch.cuda.stream(stream):
+                order = cost_model.order(feat_dev, zeros_dev, zeros_dev)
+                ctx.solve_ordered(d_q.data_ptr(), n, wl.params, order.data_ptr(), d_r.data_ptr(), d_c.data_ptr(),
+                                  CONTACT_SLOTS, stream=stream.cuda_stream)
+
+        if learned_info["used"]:  # a model that does not rank held-out costs leaves the geometric order
+            step = learned_step
 
     for _ in range(args.warmup):
         step()
@@ -313,6 +353,24 @@ def main():
     if dist:
         dist.barrier()
     launches = ctx.launches() - launches0
+    if learned_info is not None:  # the geometric order on the same batch, for the comparison
+        launches += 6 * args.steps  # the network per step: assembly, four GEMMs, expected bucket
+        res_learned = d_r.cpu().numpy().copy()
+        plain_step()
+        stream.synchronize()
+        pm = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a_ev.record(stream)
+            plain_step()
+            b_ev.record(stream)
+            stream.synchronize()
+            pm.append(a_ev.elapsed_time(b_ev))
+        learned_info["geometric_order_ms_per_step"] = float(np.mean(pm))
+        learned_info["geometric_order_value"] = n * args.steps / (sum(pm) / 1000.0)
+        learned_info["identical_results"] = bool(np.array_equal(res_learned, d_r.cpu().numpy()))
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = float(sum(step_ms))
     t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
@@ -391,6 +449,7 @@ def main():
                 "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
                 "config": config_dict(wl, args), "clocks": clk, "gpu_launches": launches, "e2e": e2e,
                 "roofline": roofline, "cpu_baseline": cpu,
+                "learned_order": learned_info,
                 "collision_fraction": float(1 - res["collisionfree"].mean()),
                 "mean_numCA": float(res["numCA"].mean()), "step_ms": step_ms}
         print(json.dumps(line), flush=True)

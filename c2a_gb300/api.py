@@ -40,7 +40,7 @@ QUERY_BAD_INPUT, QUERY_STACK_OVERFLOW, QUERY_CONTACT_OVERFLOW, QUERY_ITER_CAP = 
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
                "c2a_model_info", "c2a_model_download", "c2a_model_free", "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
-               "c2a_distance_batch", "c2a_solve_batch_hinted",
+               "c2a_distance_batch", "c2a_solve_batch_hinted", "c2a_solve_batch_ordered",
                "c2a_motion_setup", "c2a_motion_integrate"]
 
 
@@ -111,6 +111,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_toc_step_batch": ([vp, vp, i32, vp, vp, vp, C.POINTER(Params), vp], i32),
         "c2a_contact_only_batch": ([vp, vp, i32, vp, i32, vp, vp], i32),
         "c2a_distance_batch": ([vp, vp, i32, vp], i32),
+        "c2a_solve_batch_ordered": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp, vp], i32),
         "c2a_motion_setup": ([vp, vp, vp, vp, vp], i32),
         "c2a_motion_integrate": ([vp, vp, vp, vp, dbl, vp, vp, vp], i32),
     }
@@ -260,6 +261,16 @@ class Context:
                                                C.c_void_p(d_results),
                                                C.c_void_p(d_contacts) if d_contacts else None,
                                                C.c_void_p(stream) if stream else None), "c2a_solve_batch_device")
+
+    def solve_ordered(self, d_queries: int, n: int, params: dict, d_order: int, d_results: int,
+                      d_contacts: int | None, contacts_per_query: int, stream: int | None = None):
+        """c2a_solve_batch_ordered: REFERENCE mode, queries taken in the order of the
+        device int32 permutation at d_order (results as for solve_device)."""
+        prm = make_params(params, contacts_per_query)
+        _check(self.lib.c2a_solve_batch_ordered(self.h, C.c_void_p(d_queries), n, C.byref(prm), C.c_void_p(d_order),
+                                                C.c_void_p(d_results),
+                                                C.c_void_p(d_contacts) if d_contacts else None,
+                                                C.c_void_p(stream) if stream else None), "c2a_solve_batch_ordered")
 
     def solve_noalloc(self, d_queries: int, n: int, params: dict, d_results: int, d_contacts: int | None,
                       contacts_per_query: int, stream: int | None = None):

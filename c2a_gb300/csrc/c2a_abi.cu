@@ -376,7 +376,11 @@ __global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel
         if (lane == 0) q = atomicAdd(counter, 1u);
         q = __shfl_sync(kFullMask, q, 0);
         if (q >= (unsigned int)n) break;
-        if (order) q = (unsigned int)order[q];
+        if (order) {
+            const int32_t o = order[q];
+            if (o < 0 || o >= n) continue; /* not a valid query index: skipped */
+            q = (unsigned int)o;
+        }
         c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
         solve_query_warp(queries[q], models, num_models, prm, results[q], cq, mine, tstack, (int)q, lane);
     }
@@ -699,13 +703,24 @@ c2a_status c2a_model_free(c2a_context *ctx, int32_t id)
 
 namespace {
 c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
-                        c2a_result *d_results, c2a_contact *d_contacts, void *stream, const uint32_t *hints, int nh);
+                        c2a_result *d_results, c2a_contact *d_contacts, void *stream, const uint32_t *hints, int nh,
+                        const int32_t *user_order = nullptr);
 }
 
 c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
                                   c2a_result *d_results, c2a_contact *d_contacts, void *stream)
 {
     return solve_device(ctx, d_queries, n, params, d_results, d_contacts, stream, nullptr, 0);
+}
+
+c2a_status c2a_solve_batch_ordered(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
+                                   const c2a_params *params, const int32_t *d_order, c2a_result *d_results,
+                                   c2a_contact *d_contacts, void *stream)
+{
+    if (!params || params->mode != C2A_MODE_REFERENCE ||
+        (params->engine != C2A_ENGINE_AUTO && params->engine != C2A_ENGINE_WARP) || (n > 0 && !d_order))
+        return C2A_ERR_INVALID_ARGUMENT;
+    return solve_device(ctx, d_queries, n, params, d_results, d_contacts, stream, nullptr, 0, d_order);
 }
 
 c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
@@ -720,7 +735,8 @@ c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, 
 
 namespace {
 c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
-                        c2a_result *d_results, c2a_contact *d_contacts, void *stream, const uint32_t *hints, int nh)
+                        c2a_result *d_results, c2a_contact *d_contacts, void *stream, const uint32_t *hints, int nh,
+                        const int32_t *user_order)
 {
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
@@ -782,13 +798,17 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
             C2A_CUDA(cudaMalloc(&ctx->d_order, sizeof(int32_t) * (size_t)n));
             ctx->order_cap = (size_t)n;
         }
-        C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 1, 0, 2 * sizeof(unsigned int), s));
-        c2a_schedule_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(),
-                                                             ctx->d_order, ctx->d_counter + 1);
+        if (!user_order) { /* queries whose bounding spheres approach go first */
+            C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 1, 0, 2 * sizeof(unsigned int), s));
+            c2a_schedule_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_queries, n, ctx->d_models,
+                                                                 (int)ctx->models.size(), ctx->d_order,
+                                                                 ctx->d_counter + 1);
+            ctx->launches++;
+        }
         c2a_solve_warp_kernel<<<need < most ? need : most, kThreads, smem, s>>>(
             d_queries, n, ctx->d_models, (int)ctx->models.size(), prm, d_results, d_contacts, ctx->d_counter,
-            ctx->d_order, cap);
-        ctx->launches += 2;
+            user_order ? user_order : ctx->d_order, cap);
+        ctx->launches++;
         C2A_CUDA(cudaGetLastError());
         return C2A_OK;
     }

@@ -228,6 +228,25 @@ __global__ void __launch_bounds__(256) k_softmax_xent(const float *__restrict__ 
     if (threadIdx.x == 0) loss[m] = logf(s) + mx - x[lab];
 }
 
+/* the expected class index of a row under its softmax */
+__global__ void __launch_bounds__(256) k_expect(const float *__restrict__ logits, int N, float *__restrict__ out)
+{
+    __shared__ float sh[32];
+    const float *x = logits + (size_t)blockIdx.x * N;
+    float mx = -INFINITY;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) mx = fmaxf(mx, x[n]);
+    mx = block_reduce(mx, sh, true);
+    float s0 = 0.0f, s1 = 0.0f;
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        const float e = expf(x[n] - mx);
+        s0 += e;
+        s1 += e * (float)n;
+    }
+    s0 = block_reduce(s0, sh, false);
+    s1 = block_reduce(s1, sh, false);
+    if (threadIdx.x == 0) out[blockIdx.x] = s1 / s0;
+}
+
 /* column sums: block = 32 columns x 8 row groups */
 __global__ void k_colsum(const uint16_t *__restrict__ in, int M, int N, float *__restrict__ out)
 {
@@ -379,6 +398,13 @@ c2a_status c2a_mlp_softmax_xent(const float *logits, const int32_t *labels, int3
 {
     if (!logits || !labels || !loss || !d_logits || M <= 0 || N <= 0) return C2A_ERR_INVALID_ARGUMENT;
     k_softmax_xent<<<M, 256, 0, (cudaStream_t)stream>>>(logits, labels, N, scale, loss, d_logits);
+    return launch_status();
+}
+
+c2a_status c2a_mlp_expect(const float *logits, int32_t M, int32_t N, float *out, void *stream)
+{
+    if (!logits || !out || M <= 0 || N <= 0) return C2A_ERR_INVALID_ARGUMENT;
+    k_expect<<<M, 256, 0, (cudaStream_t)stream>>>(logits, N, out);
     return launch_status();
 }
 

@@ -41,7 +41,7 @@ OUT = NCLUSTER * NCLUSTER
 TOPK = 8
 ROW_ALIGN = 128
 
-MLP_SYMBOLS = ["c2a_mlp_adam", "c2a_mlp_assemble", "c2a_mlp_colsum", "c2a_mlp_embed_backward",
+MLP_SYMBOLS = ["c2a_mlp_adam", "c2a_mlp_assemble", "c2a_mlp_colsum", "c2a_mlp_embed_backward", "c2a_mlp_expect",
                "c2a_mlp_gelu_backward", "c2a_mlp_gemm", "c2a_mlp_softmax_xent", "c2a_mlp_topk",
                "c2a_mlp_transpose"]
 
@@ -61,6 +61,7 @@ def bind(lib=None):
         "c2a_mlp_assemble": [vp, vp, vp, vp, i32, i32, i32, vp, vp],
         "c2a_mlp_embed_backward": [vp, vp, vp, i32, i32, vp, vp],
         "c2a_mlp_topk": [vp, i32, i32, i32, vp, vp],
+        "c2a_mlp_expect": [vp, i32, i32, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -474,3 +475,50 @@ def experiment(n_train: int = 2_000_000, n_eval: int = 65536, epochs: int = 4, p
         log(f"CANONICAL engine {engine}: plain {ms_plain:.1f} ms, hinted {ms_hint:.1f} ms "
             f"({out['speedup']:.3f}x), identical results: {out['identical']}")
     return out
+
+
+# ------------------------------------------------------------ learned schedule
+
+COST_BUCKETS = 64
+LEAF_COST = 1.6  # a leaf pair (TriDist on the warp) against an expansion, from the profiling build's cycle counters
+
+
+def query_cost(results: np.ndarray) -> np.ndarray:
+    """A REFERENCE query's work in expansions: num_bv_tests / 2 node-pair
+    expansions plus the triangle tests weighted by their relative cost."""
+    return results["num_bv_tests"] / 2.0 + LEAF_COST * results["num_tri_tests"]
+
+
+class CostOrder:
+    """Learned schedule for REFERENCE batches: the same network, trained to
+    classify a query's log-cost into 64 buckets from its pose features;
+    queries are then taken in decreasing expected bucket (the costliest
+    first), which shortens a batch whose length is set by its heaviest
+    queries.  The order never changes a result (c2a_solve_batch_ordered)."""
+
+    def __init__(self, num_meshes: int = 1, seed: int = 0):
+        self.net = SeedNet(num_meshes, seed=seed)
+        self.top = 1.0
+
+    def fit(self, feat, ia, ib, cost, epochs: int = 10, batch: int = 1024, log=None) -> list[float]:
+        y = np.log1p(np.asarray(cost, dtype=np.float64))
+        self.top = float(y.max()) if y.max() > 0 else 1.0
+        lab = np.minimum((y / self.top * (COST_BUCKETS - 1)).astype(np.int32), COST_BUCKETS - 1)
+        return self.net.train(feat, ia, ib, lab, epochs=epochs, batch=batch, log=log)
+
+    def expected(self, feat_dev, ia_dev, ib_dev):
+        """Expected cost bucket of each query (device FP32); inputs on the device."""
+        torch = self.net.torch
+        n = feat_dev.shape[0]
+        M = (n + ROW_ALIGN - 1) // ROW_ALIGN * ROW_ALIGN
+        x = self.net.assemble(feat_dev, ia_dev, ib_dev, M)
+        logits = self.net.forward(x)
+        out = torch.empty(M, dtype=torch.float32, device=self.net.dev)
+        _ok(self.net.lib.c2a_mlp_expect(_p(logits), M, OUT, _p(out), self.net._s()), "c2a_mlp_expect")
+        return out[:n]
+
+    def order(self, feat_dev, ia_dev, ib_dev):
+        """The schedule: query indices by decreasing expected cost (device int32)."""
+        torch = self.net.torch
+        e = self.expected(feat_dev, ia_dev, ib_dev)
+        return torch.argsort(e, descending=True, stable=True).to(torch.int32)

@@ -236,6 +236,17 @@ c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, in
 /* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]
  * angular speed, out[4:7] linear velocity, out[7:11] begin quaternion
  * (x, y, z, w). */
+/* c2a_solve_batch_device in C2A_MODE_REFERENCE (engine AUTO or WARP) taking
+ * the queries in the caller's order: d_order (device int32) holds a
+ * permutation of [0, n); entries outside [0, n) are skipped.  The order only
+ * decides which warp takes which query when (a schedule that starts the
+ * costliest queries first shortens the batch); every result equals the
+ * unordered call's.  The learned cost model of c2a_gb300/learned.py
+ * produces such orders. */
+c2a_status c2a_solve_batch_ordered(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
+                                   const c2a_params *params, const int32_t *d_order, c2a_result *d_results,
+                                   c2a_contact *d_contacts, void *stream);
+
 /* c2a_solve_batch_device in C2A_MODE_CANONICAL with hints: d_hints holds, per
  * query, hints_per_query (<= 16) pairs of hinted BVH nodes (model a's, then
  * model b's), each encoded as its path from the root in the low 16 bits (bit

@@ -10,6 +10,8 @@
  *        embeddings) -> 256 -> 256 -> 256 -> 4096 logits (64 x 64 cluster pairs),
  *
  * GELU after each hidden layer, trained with softmax cross-entropy and Adam.
+ * The same network, trained on 64 log-cost buckets, orders REFERENCE batches
+ * so that the costliest queries start first (c2a_solve_batch_ordered).
  * These entry points are the building blocks (tensor-core GEMM with fused
  * epilogues, the loss, the optimizer step, top-k); c2a_gb300/learned.py
  * composes them into training and inference.
@@ -53,6 +55,9 @@ c2a_status c2a_mlp_gelu_backward(const float *d_act, const float *pre, int64_t c
  * ignored rows (zero loss and gradient) */
 c2a_status c2a_mlp_softmax_xent(const float *logits, const int32_t *labels, int32_t M, int32_t N, float scale,
                                 float *loss, uint16_t *d_logits, void *stream);
+
+/* out[m] = sum_n softmax(logits[m])[n] * n: the expected class index of each row */
+c2a_status c2a_mlp_expect(const float *logits, int32_t M, int32_t N, float *out, void *stream);
 
 /* out[n] = sum_m in[m][n] (FP32; in is bf16, M x N) */
 c2a_status c2a_mlp_colsum(const uint16_t *in, int32_t M, int32_t N, float *out, void *stream);

@@ -217,3 +217,61 @@ def test_gpu_hinted_solve_equals_plain(gpu_ctx, engine):
         b = hc[i * 128:i * 128 + n]
         for f in ("tri_a", "tri_b", "distance", "pa", "pb"):
             assert bits(a[f]) == bits(b[f]), (i, f)
+
+
+@pytest.mark.gpu
+def test_gpu_ordered_solve_equals_plain(gpu_ctx):
+    import torch
+
+    wl = workloads.small_knots(300, seed=61)
+    mid = gpu_ctx.model(wl.meshes[0])
+    q = wl.qint.copy()
+    q[:, :2] = mid
+    plain, pc = gpu_ctx.solve(q, wl.poses, wl.params, contacts_per_query=64)
+    qs = api.make_queries(q, wl.poses)
+    n = len(qs)
+    d_q = torch.from_numpy(qs.view(np.uint8).copy()).cuda()
+    for order in (np.random.default_rng(62).permutation(n), np.arange(n)[::-1].copy()):
+        d_o = torch.tensor(order.astype(np.int32), device="cuda")
+        d_r = torch.zeros(n * api.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        d_c = torch.zeros(n * 64 * api.CONTACT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        gpu_ctx.solve_ordered(d_q.data_ptr(), n, wl.params, d_o.data_ptr(), d_r.data_ptr(), d_c.data_ptr(), 64)
+        torch.cuda.synchronize()
+        r = d_r.cpu().numpy().view(api.RESULT_DTYPE)
+        c = d_c.cpu().numpy().view(api.CONTACT_DTYPE)
+        for f in RESULT_FIELDS:
+            assert bits(plain[f]) == bits(r[f]), f
+        for i in range(n):
+            m = min(int(plain[i]["num_contact"]), 64)
+            for f in ("tri_a", "tri_b", "distance", "pa", "pb"):
+                assert bits(pc[i][:m][f]) == bits(c[i * 64:i * 64 + m][f]), (i, f)
+    # entries outside [0, n) are skipped, not read
+    d_o = torch.tensor(np.r_[np.arange(n - 2), -1, n].astype(np.int32), device="cuda")
+    d_r = torch.zeros(n * api.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    gpu_ctx.solve_ordered(d_q.data_ptr(), n, wl.params, d_o.data_ptr(), d_r.data_ptr(), None, 0)
+    torch.cuda.synchronize()
+    r = d_r.cpu().numpy().view(api.RESULT_DTYPE)
+    assert bits(r["toc"][: n - 2]) == bits(plain["toc"][: n - 2]) and (r["numCA"][n - 2:] == 0).all()
+
+
+@pytest.mark.gpu
+def test_gpu_cost_order_learns(gpu_ctx):
+    """The cost model's training and inference path on a cost that is a known
+    function of two features (its predictive power on real CA costs is what
+    bench.py measures on held-out queries)."""
+    import torch
+
+    rng = np.random.default_rng(63)
+    n = 8192
+    feat = rng.normal(size=(n, 18)).astype(np.float32)
+    cost = np.exp(3.0 * feat[:, 12] + 2.0 * feat[:, 13] + 6.0)
+    z = np.zeros(n, np.int32)
+    model = learned.CostOrder(1, seed=2)
+    hist = model.fit(feat[:6144], z[:6144], z[:6144], cost[:6144], epochs=40, batch=512)
+    assert hist[-1] < 0.8 * hist[0], hist
+    dev = lambda a: torch.tensor(a, device="cuda")
+    e = model.expected(dev(feat[6144:]), dev(z[6144:]), dev(z[6144:])).cpu().numpy()
+    r = np.corrcoef(np.argsort(np.argsort(e)), np.argsort(np.argsort(cost[6144:])))[0, 1]
+    assert r > 0.8, r  # held-out rank correlation of predicted and true cost
+    o = model.order(dev(feat), dev(z), dev(z)).cpu().numpy()
+    assert sorted(o.tolist()) == list(range(n))
