@@ -354,7 +354,8 @@ def main():
         dist.barrier()
     launches = ctx.launches() - launches0
     if learned_info is not None:  # the geometric order on the same batch, for the comparison
-        launches += 6 * args.steps  # the network per step: assembly, four GEMMs, expected bucket
+        if learned_info["used"]:
+            launches += 6 * args.steps  # the network per step: assembly, four GEMMs, expected bucket
         res_learned = d_r.cpu().numpy().copy()
         plain_step()
         stream.synchronize()
