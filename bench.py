@@ -311,14 +311,15 @@ def main():
         cut = (wl_tr.n * 4 // 5) // 1024 * 1024  # 80 % to train on, the rest held out
         cost_model = learned.CostOrder(1, seed=rank)
         zeros_tr = np.zeros(wl_tr.n, dtype=np.int32)
-        hist = cost_model.fit(f_tr[:cut], zeros_tr[:cut], zeros_tr[:cut], cost_tr[:cut], epochs=30)
+        epochs = max(30, -(-1536 // max(cut // 1024, 1)))  # about 1,500 optimizer steps whatever the batch size
+        hist = cost_model.fit(f_tr[:cut], zeros_tr[:cut], zeros_tr[:cut], cost_tr[:cut], epochs=epochs)
         held = cost_model.expected(torch.tensor(f_tr[cut:], device="cuda"), torch.tensor(zeros_tr[cut:], device="cuda"),
                                    torch.tensor(zeros_tr[cut:], device="cuda")).cpu().numpy()
         rank_r = float(np.corrcoef(np.argsort(np.argsort(held)), np.argsort(np.argsort(cost_tr[cut:])))[0, 1])
         feat_dev = torch.tensor(learned.features(wl.poses, np.full(n, diag), np.full(n, diag)), device="cuda")
         zeros_dev = torch.zeros(n, dtype=torch.int32, device="cuda")
         learned_info = {"train_queries": cut, "held_out_queries": wl_tr.n - cut, "train_seed": 1000 + rank,
-                        "epochs": 30, "final_loss": hist[-1], "held_out_rank_correlation": rank_r,
+                        "epochs": epochs, "final_loss": hist[-1], "held_out_rank_correlation": rank_r,
                         "used": rank_r >= 0.6, "setup_s": time.time() - t_setup}
 
         def learned_step():
@@ -413,13 +414,31 @@ def main():
 
     e2e = None
     if not args.no_e2e:
-        rr, cc = ctx.solve(qint, wl.poses, wl.params, contacts_per_query=CONTACT_SLOTS)  # warm the host path
+        h2d_extra = 0
+        if learned_info is not None and learned_info["used"]:
+            # the learned pipeline from host memory: features H2D, the network's order on the device, then
+            # the ordered host-buffer call (queries H2D, results and dense contacts D2H)
+            h_feat = torch.from_numpy(learned.features(wl.poses, np.full(n, diag), np.full(n, diag))).pin_memory()
+            h2d_extra = h_feat.numel() * 4
+
+            def e2e_call():
+                with torch.cuda.stream(stream):
+                    feat_dev.copy_(h_feat, non_blocking=True)
+                    order = cost_model.order(feat_dev, zeros_dev, zeros_dev)
+                stream.synchronize()
+                return ctx.solve_ordered_host(qint, wl.poses, wl.params, order.data_ptr(),
+                                              contacts_per_query=CONTACT_SLOTS)
+        else:
+            def e2e_call():
+                return ctx.solve(qint, wl.poses, wl.params, contacts_per_query=CONTACT_SLOTS)
+
+        rr, cc = e2e_call()  # warm the host path
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
         totals = []
         for _ in range(args.steps):
-            rr, cc = ctx.solve(qint, wl.poses, wl.params, contacts_per_query=CONTACT_SLOTS)
+            rr, cc = e2e_call()
             totals.append(cc.total())
         e2e_s = time.perf_counter() - t0
         te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
@@ -427,10 +446,11 @@ def main():
             dist.all_reduce(te, op=dist.ReduceOp.MAX)
         e2e_s = float(te.item())
         e2e = {"value": n * world * args.steps / e2e_s, "unit": UNIT,
-               "h2d_bytes_per_step": n * api.QUERY_DTYPE.itemsize,
+               "h2d_bytes_per_step": n * api.QUERY_DTYPE.itemsize + h2d_extra,
                "d2h_bytes_per_step": int(n * api.RESULT_DTYPE.itemsize + np.mean(totals) * api.CONTACT_DTYPE.itemsize
                                          + 4),
-               "api": "c2a_solve_batch (host buffers)"}
+               "api": ("c2a_solve_batch_ordered_host (host buffers; the order from the network on the device)"
+                       if h2d_extra else "c2a_solve_batch (host buffers)")}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -41,6 +41,7 @@ ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count"
                "c2a_model_info", "c2a_model_download", "c2a_model_free", "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
                "c2a_distance_batch", "c2a_solve_batch_hinted", "c2a_solve_batch_ordered",
+               "c2a_solve_batch_ordered_host",
                "c2a_motion_setup", "c2a_motion_integrate"]
 
 
@@ -112,6 +113,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_contact_only_batch": ([vp, vp, i32, vp, i32, vp, vp], i32),
         "c2a_distance_batch": ([vp, vp, i32, vp], i32),
         "c2a_solve_batch_ordered": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp, vp], i32),
+        "c2a_solve_batch_ordered_host": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp], i32),
         "c2a_motion_setup": ([vp, vp, vp, vp, vp], i32),
         "c2a_motion_integrate": ([vp, vp, vp, vp, dbl, vp, vp, vp], i32),
     }
@@ -252,6 +254,21 @@ class Context:
         if check:
             _check(s, "c2a_distance_batch")
         return res
+
+    def solve_ordered_host(self, qint: np.ndarray, poses: np.ndarray, params: dict, d_order: int,
+                           contacts_per_query: int = 64, check: bool = True):
+        """c2a_solve_batch_ordered_host: as solve(), with the queries taken in the order of
+        the device int32 permutation at d_order (REFERENCE mode)."""
+        q = make_queries(qint, poses)
+        n = len(q)
+        res = np.zeros(n, dtype=RESULT_DTYPE)
+        con = np.zeros(max(1, n * contacts_per_query), dtype=CONTACT_DTYPE)
+        prm = make_params(params, contacts_per_query)
+        s = self.lib.c2a_solve_batch_ordered_host(self.h, _ptr(q), n, C.byref(prm), C.c_void_p(d_order), _ptr(res),
+                                                  _ptr(con) if contacts_per_query > 0 else None)
+        if check:
+            _check(s, "c2a_solve_batch_ordered_host")
+        return res, Contacts(con, res, contacts_per_query)
 
     def solve_device(self, d_queries: int, n: int, params: dict, d_results: int, d_contacts: int | None,
                      contacts_per_query: int, stream: int | None = None):

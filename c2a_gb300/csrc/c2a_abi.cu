@@ -860,8 +860,11 @@ c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_
     return C2A_OK;
 }
 
-c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const c2a_params *params,
-                           c2a_result *results, c2a_contact *contacts)
+namespace {
+/* the host-buffer entry points: queries in, the batch (in the caller's device
+ * order when d_order is given), results and dense contacts out */
+c2a_status solve_host(c2a_context *ctx, const c2a_query *queries, int32_t n, const c2a_params *params,
+                      c2a_result *results, c2a_contact *contacts, const int32_t *d_order)
 {
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!queries || !results))) return C2A_ERR_INVALID_ARGUMENT;
@@ -885,7 +888,8 @@ c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n
     C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
     c2a_params prm = *params;
     if (!cpq) prm.contacts_per_query = 0;
-    st = c2a_solve_batch_device(ctx, dq, n, &prm, dr, dc, ctx->stream);
+    st = d_order ? c2a_solve_batch_ordered(ctx, dq, n, &prm, d_order, dr, dc, ctx->stream)
+                 : c2a_solve_batch_device(ctx, dq, n, &prm, dr, dc, ctx->stream);
     if (st) return st;
     int32_t total = 0;
     if (cpq) {
@@ -907,6 +911,21 @@ c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n
     for (int32_t i = 0; i < n; i++)
         if (results[i].status & ~(C2A_QUERY_ITER_CAP | C2A_QUERY_CONTACT_OVERFLOW)) return C2A_ERR_QUERY_FAILED;
     return C2A_OK;
+}
+} // namespace
+
+c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const c2a_params *params,
+                           c2a_result *results, c2a_contact *contacts)
+{
+    return solve_host(ctx, queries, n, params, results, contacts, nullptr);
+}
+
+c2a_status c2a_solve_batch_ordered_host(c2a_context *ctx, const c2a_query *queries, int32_t n,
+                                        const c2a_params *params, const int32_t *d_order, c2a_result *results,
+                                        c2a_contact *contacts)
+{
+    if (n > 0 && !d_order) return C2A_ERR_INVALID_ARGUMENT;
+    return solve_host(ctx, queries, n, params, results, contacts, d_order);
 }
 
 c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries, int32_t n,

@@ -247,6 +247,14 @@ c2a_status c2a_solve_batch_ordered(c2a_context *ctx, const c2a_query *d_queries,
                                    const c2a_params *params, const int32_t *d_order, c2a_result *d_results,
                                    c2a_contact *d_contacts, void *stream);
 
+/* c2a_solve_batch (host buffers in and out, dense contacts) taking the
+ * queries in the order of d_order, a permutation of [0, n) in device memory
+ * (it usually comes from a device-side cost model); REFERENCE mode, engine
+ * AUTO or WARP.  Results equal c2a_solve_batch's. */
+c2a_status c2a_solve_batch_ordered_host(c2a_context *ctx, const c2a_query *queries, int32_t n,
+                                        const c2a_params *params, const int32_t *d_order, c2a_result *results,
+                                        c2a_contact *contacts);
+
 /* c2a_solve_batch_device in C2A_MODE_CANONICAL with hints: d_hints holds, per
  * query, hints_per_query (<= 16) pairs of hinted BVH nodes (model a's, then
  * model b's), each encoded as its path from the root in the low 16 bits (bit

@@ -245,6 +245,13 @@ def test_gpu_ordered_solve_equals_plain(gpu_ctx):
             m = min(int(plain[i]["num_contact"]), 64)
             for f in ("tri_a", "tri_b", "distance", "pa", "pb"):
                 assert bits(pc[i][:m][f]) == bits(c[i * 64:i * 64 + m][f]), (i, f)
+        # the host-buffer form: dense contacts as c2a_solve_batch returns them
+        rh, ch = gpu_ctx.solve_ordered_host(q, wl.poses, wl.params, d_o.data_ptr(), contacts_per_query=64)
+        for f in RESULT_FIELDS + ["contact_offset"]:
+            assert bits(plain[f]) == bits(rh[f]), f
+        for i in range(n):
+            for f in ("tri_a", "tri_b", "distance", "pa", "pb"):
+                assert bits(pc[i][f]) == bits(ch[i][f]), (i, f)
     # entries outside [0, n) are skipped, not read
     d_o = torch.tensor(np.r_[np.arange(n - 2), -1, n].astype(np.int32), device="cuda")
     d_r = torch.zeros(n * api.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
