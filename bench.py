@@ -212,7 +212,8 @@ def config_dict(wl, args, sample_only=None):
             "mode": args.mode, "engine": args.engine, "traversal": traversal,
             "seeding": "plain (triangle 0 of each model, as after EndModel); the learned seeding is measured "
                        "by --mode learned (CANONICAL mode only: REFERENCE results depend on the seed)",
-            "order": args.order if args.mode == "reference" else "geometric",
+            "order": ("not applicable: the CPU port, queries split statically over the threads"
+                      if args.impl == "reference" else args.order if args.mode == "reference" else "geometric"),
             "contacts_per_query": CONTACT_SLOTS, "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": f"replicas x{args.gpus}"}
 
