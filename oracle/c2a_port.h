@@ -1,7 +1,8 @@
 /*
  * c2a_port.h -- CPU oracle: a plain-C restatement of C2A's controlled
- * conservative advancement (CA) path, used by the tests, smoke() and the
- * bench's CPU baseline as the checker.  Nothing in the product links it.
+ * conservative advancement (CA) path; test infrastructure, used by the
+ * tests, smoke() and the bench's CPU baseline to verify and time the CUDA
+ * path.  Nothing in the product links it.
  *
  * It follows the reference function by function (file:line in each
  * definition): the RSS BVH build (C2A/src/C2A_Build.cpp, C2A/src/C2A_BV.cpp),

@@ -1,5 +1,5 @@
 """CPU oracle of the learned seeding's network (test infrastructure: only the
-tests import it, as the checker of the CUDA kernels in c2a_gb300/csrc/mlp.cu).
+tests import it, to verify the CUDA kernels in c2a_gb300/csrc/mlp.cu).
 
 A numpy restatement of the forward and backward passes with BF16 rounding at
 the points where the CUDA path rounds (inputs, weight copies, hidden
