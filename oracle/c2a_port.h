@@ -78,6 +78,13 @@ enum { C2A_PORT_MODE_REFERENCE = 0, C2A_PORT_MODE_CANONICAL = 1 };
 double c2a_port_distance(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
                          int seed_a, int seed_b, int *ta, int *tb, long long *nbv, long long *ntri);
 
+/* C2A_Tolerance (qsize 2) with B placed in A's frame by (R, T): returns
+ * closer_than_tolerance; when set, the distance and closest points (p1 in
+ * A's frame, p2 in B's) of the first pair found within the tolerance */
+int c2a_port_tolerance(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
+                       double tolerance, double *distance, double p1[3], double p2[3], long long *nbv,
+                       long long *ntri);
+
 typedef struct c2a_port_contact {
     int type_a, type_b;  /* 1 vertex, 2 edge, 3 face (C2A.cpp:1584-1585) */
     int fid_a[3], fid_b[3]; /* vertex indices of the features, -1 unused */

@@ -418,6 +418,97 @@ double c2a_port_distance(const c2a_port_model *A, const c2a_port_model *B, const
     return distance_query(A, B, (const double(*)[3])Rm, T, seed_a, seed_b, ta, tb, nbv, ntri);
 }
 
+/* ------------------------------------------------------- tolerance query */
+
+typedef struct tol_state {
+    const c2a_port_model *o1, *o2;
+    double R[3][3], T[3]; /* model 2 relative to model 1 */
+    double tolerance, distance, p1[3], p2[3];
+    int closer;
+    long long num_bv_tests, num_tri_tests;
+} tol_state;
+
+/* C2AToleranceRecurse, C2A/src/C2A_PQP.cpp:1498-1603: depth first, the pair
+ * with the smaller RSS distance first, stopping at the first triangle pair
+ * within the tolerance */
+static void tol_recurse(tol_state *ts, const double R[3][3], const double T[3], int b1, int b2)
+{
+    const c2a_port_node *n1 = &ts->o1->nodes[b1], *n2 = &ts->o2->nodes[b2];
+    int l1 = n1->first_child < 0, l2 = n2->first_child < 0;
+    if (l1 && l2) {
+        double p[3], q[3], d;
+        int ia = -n1->first_child - 1, ib = -n2->first_child - 1;
+        ts->num_tri_tests++;
+        d = tri_distance_plain((const double(*)[3])ts->R, ts->T, &ts->o1->tris[ia], &ts->o2->tris[ib], p, q);
+        if (d <= ts->tolerance) {
+            ts->closer = 1;
+            ts->distance = d;
+            pv_copy(ts->p1, p);
+            pv_copy(ts->p2, q);
+        }
+        return;
+    }
+    {
+        int a1, a2, c1, c2;
+        double R1[3][3], T1[3], R2[3][3], T2[3], S[3], d1, d2;
+        step_state cs;
+        cs.o1 = ts->o1;
+        cs.o2 = ts->o2;
+        children(&cs, b1, b2, R, T, &a1, &a2, &c1, &c2, R1, T1, R2, T2);
+        ts->num_bv_tests += 2;
+        d1 = bv_distance((const double(*)[3])R1, T1, &ts->o1->nodes[a1], &ts->o2->nodes[a2], S);
+        d2 = bv_distance((const double(*)[3])R2, T2, &ts->o1->nodes[c1], &ts->o2->nodes[c2], S);
+        if (d2 < d1) {
+            if (d2 <= ts->tolerance) tol_recurse(ts, (const double(*)[3])R2, T2, c1, c2);
+            if (ts->closer) return;
+            if (d1 <= ts->tolerance) tol_recurse(ts, (const double(*)[3])R1, T1, a1, a2);
+        } else {
+            if (d1 <= ts->tolerance) tol_recurse(ts, (const double(*)[3])R1, T1, a1, a2);
+            if (ts->closer) return;
+            if (d2 <= ts->tolerance) tol_recurse(ts, (const double(*)[3])R2, T2, c1, c2);
+        }
+    }
+}
+
+/* C2A_Tolerance with qsize 2 (C2A_PQP.cpp:1762-1845): the root RSS distance
+ * as a trivial reject, then the recursion; p2 back into model 2's frame */
+int c2a_port_tolerance(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
+                       double tolerance, double *distance, double p1[3], double p2[3], long long *nbv,
+                       long long *ntri)
+{
+    tol_state ts;
+    double Rm[3][3], Rtemp[3][3], Rr[3][3], Ttemp[3], Tr[3], S[3], u[3], d;
+    const c2a_port_node *r1 = &A->nodes[0], *r2 = &B->nodes[0];
+    pm_from9(Rm, R);
+    ts.o1 = A;
+    ts.o2 = B;
+    pm_copy(ts.R, (const double(*)[3])Rm);
+    pv_copy(ts.T, T);
+    if (tolerance < 0.0) tolerance = 0.0;
+    ts.tolerance = tolerance;
+    ts.num_bv_tests = ts.num_tri_tests = 0;
+    ts.closer = 0;
+    ts.distance = 0.0;
+    ts.p1[0] = ts.p1[1] = ts.p1[2] = 0.0;
+    ts.p2[0] = ts.p2[1] = ts.p2[2] = 0.0;
+    pm_mul(Rtemp, (const double(*)[3])Rm, (const double(*)[3])r2->R);
+    pm_tmul(Rr, (const double(*)[3])r1->R, (const double(*)[3])Rtemp);
+    pm_mul_v_add(Ttemp, (const double(*)[3])Rm, r2->Tr, T);
+    pv_sub(Ttemp, Ttemp, r1->Tr);
+    pm_tmul_v(Tr, (const double(*)[3])r1->R, Ttemp);
+    d = bv_distance((const double(*)[3])Rr, Tr, r1, r2, S);
+    if (d <= ts.tolerance) tol_recurse(&ts, (const double(*)[3])Rr, Tr, 0, 0);
+    if (ts.closer) {
+        pv_sub(u, ts.p2, T);
+        pm_tmul_v(p2, (const double(*)[3])Rm, u);
+        pv_copy(p1, ts.p1);
+        *distance = ts.distance;
+    }
+    if (nbv) *nbv = ts.num_bv_tests;
+    if (ntri) *ntri = ts.num_tri_tests;
+    return ts.closer;
+}
+
 /* -------------------------------------------------- translation-only CA */
 
 /* CInterpMotion_Linear::CAonNonAdjacentTriangles, InterpMotion.cpp:657-743 */

@@ -92,6 +92,9 @@ class Port:
         L.c2a_port_distance.argtypes = [C.POINTER(_PortModel), C.POINTER(_PortModel), C.c_void_p, C.c_void_p,
                                         C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.c2a_port_distance.restype = C.c_double
+        L.c2a_port_tolerance.argtypes = [C.POINTER(_PortModel), C.POINTER(_PortModel), C.c_void_p, C.c_void_p,
+                                         C.c_double] + [C.c_void_p] * 5
+        L.c2a_port_tolerance.restype = C.c_int
 
     def models(self, meshes) -> C.Array:
         """Builds every mesh's hierarchy; returns a ctypes array of models."""
@@ -134,6 +137,17 @@ class Port:
         d = self.lib.c2a_port_distance(C.byref(models[ia]), C.byref(models[ib]), _dptr(R), _dptr(T), int(seed_a),
                                        int(seed_b), _dptr(t[0:1]), _dptr(t[1:2]), None, None)
         return d, int(t[0]), int(t[1])
+
+    def tolerance(self, models, ia: int, ib: int, R, T, tol: float):
+        """C2A_Tolerance (qsize 2): (closer, distance, p1, p2, num_bv_tests, num_tri_tests)."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(9)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(3)
+        d = np.zeros(1)
+        p1, p2 = np.zeros(3), np.zeros(3)
+        n = np.zeros(2, dtype=np.int64)
+        c = self.lib.c2a_port_tolerance(C.byref(models[ia]), C.byref(models[ib]), _dptr(R), _dptr(T), float(tol),
+                                        _dptr(d), _dptr(p1), _dptr(p2), _dptr(n[0:1]), _dptr(n[1:2]))
+        return c, float(d[0]), p1, p2, int(n[0]), int(n[1])
 
     def rectdist(self, Rab, Tab, a, b):
         Rab = np.ascontiguousarray(Rab, dtype=np.float64).reshape(9)
@@ -178,6 +192,8 @@ class Ref:
         L.c2a_ref_motion.argtypes = [C.c_void_p] * 4 + [C.c_double] + [C.c_void_p] * 3
         L.c2a_ref_distance.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_int] + [C.c_void_p] * 4
         L.c2a_ref_distance.restype = C.c_double
+        L.c2a_ref_tolerance.argtypes = [C.c_void_p] * 4 + [C.c_double, C.c_void_p]
+        L.c2a_ref_tolerance.restype = C.c_int
 
     @staticmethod
     def available() -> bool:
@@ -245,6 +261,14 @@ class Ref:
         d = self.lib.c2a_ref_distance(ha, hb, _dptr(R), _dptr(T), int(seed_a), int(seed_b), _dptr(t[0:1]),
                                       _dptr(t[1:2]), None, None)
         return d, int(t[0]), int(t[1])
+
+    def tolerance(self, ha, hb, R, T, tol: float):
+        """The reference's C2A_Tolerance (qsize 2): (closer, distance, p1, p2, num_bv_tests, num_tri_tests)."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(9)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(3)
+        out = np.zeros(9)
+        c = self.lib.c2a_ref_tolerance(ha, hb, _dptr(R), _dptr(T), float(tol), _dptr(out))
+        return c, float(out[0]), out[1:4].copy(), out[4:7].copy(), int(out[7]), int(out[8])
 
     def motion(self, R0, T0, R1, T1, t):
         args = [np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (R0, T0, R1, T1)]

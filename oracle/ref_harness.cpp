@@ -31,6 +31,10 @@ int C2A_TimeOfContactStep(CInterpMotion *objmotion1, CInterpMotion *objmotion2, 
                           PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3], PQP_REAL T2[3],
                           C2A_Model *o2, PQP_REAL tolerance_t, PQP_REAL tolerance_d);
 
+// defined in C2A/src/C2A_PQP.cpp (RSS builds) without a header declaration
+int C2A_Tolerance(PQP_ToleranceResult *res, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                  PQP_REAL T2[3], C2A_Model *o2, PQP_REAL tolerance, int qsize);
+
 extern "C" {
 
 // Same layout as c2a_port_result / c2a_port_contact (oracle/c2a_port.h).
@@ -206,6 +210,27 @@ static void closest_seed(C2A_TimeOfContactResult &dres, C2A_Model *A, C2A_Model 
   C2A_Distance(&dd, R1, T1, A, R2, T2, B, 0.0, 0.0, 2);
   dres.last_triA = A->last_tri;
   dres.last_triB = B->last_tri;
+}
+
+// C2A_Tolerance (qsize 2); R/T place model B in model A's frame.  out:
+// distance, p1[3], p2[3], num_bv_tests, num_tri_tests; returns closer_than_tolerance.
+int c2a_ref_tolerance(void *ha, void *hb, const double *R9, const double *T3, double tolerance, double *out)
+{
+  C2A_Model *A = (C2A_Model *)ha, *B = (C2A_Model *)hb;
+  PQP_REAL I[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, Z[3] = {0, 0, 0}, R[3][3], T[3];
+  m9(R, R9);
+  VcV(T, T3);
+  PQP_ToleranceResult res;
+  memset(&res, 0, sizeof(res));
+  C2A_Tolerance(&res, I, Z, A, R, T, B, tolerance, 2);
+  out[0] = res.distance;
+  for (int i = 0; i < 3; i++) {
+    out[1 + i] = res.p1[i];
+    out[4 + i] = res.p2[i];
+  }
+  out[7] = res.num_bv_tests;
+  out[8] = res.num_tri_tests;
+  return res.closer_than_tolerance;
 }
 
 // C2A_Distance (rel_err = abs_err = 0, qsize 2) from a seed pair; R/T place

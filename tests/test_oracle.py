@@ -118,3 +118,33 @@ def test_port_matches_live_reference(port, ref):
             assert bits(res[q][f]) == bits(r[f]), (q, f)
         n = int(r["num_contact"])
         assert bits(con[q][:n]) == bits(np.ascontiguousarray(c[::-1])), q
+
+
+def test_port_tolerance_matches_reference(port, ref):
+    """C2A_Tolerance (qsize 2), C2A/src/C2A_PQP.cpp:1498-1603, 1762-1845: the
+    port against the compiled reference on a knot, a soup and an icosphere,
+    with tolerances below, around and above each pair's exact distance --
+    the flag, the counters and, where a pair is found, its distance and
+    points, bit for bit."""
+    from c2a_gb300 import meshes, workloads
+
+    ms = [meshes.torus_knot(2, 3, 40, 8), meshes.triangle_soup(600, clusters=5, seed=71),
+          meshes.icosphere(2, radius=0.8, noise=0.02, seed=72)]
+    models = port.models(ms)
+    ha = [ref.model(m) for m in ms]
+    hb = [ref.model(m) for m in ms]
+    rng = np.random.default_rng(73)
+    found = 0
+    for k in range(120):
+        a, b = rng.integers(0, 3, 2)
+        R = workloads.random_rotations(rng, 1).reshape(9)
+        T = workloads.unit_vectors(rng, 1)[0] * rng.uniform(0.5, 3.0) + rng.normal(scale=1e-3, size=3)
+        d, _, _ = port.distance(models, a, b, R, T, 0, 0)
+        tol = d * rng.choice([0.5, 0.999, 1.0, 1.001, 2.0]) if d > 0 else rng.uniform(0, 0.1)
+        got = port.tolerance(models, a, b, R, T, tol)
+        exp = ref.tolerance(ha[a], hb[b], R, T, tol)
+        assert got[0] == exp[0] and got[4:] == exp[4:], (k, got, exp)
+        if exp[0]:
+            found += 1
+            assert bits(got[1]) == bits(exp[1]) and bits(got[2]) == bits(exp[2]) and bits(got[3]) == bits(exp[3]), k
+    assert 30 < found < 120
