@@ -4,18 +4,23 @@
  * counters), while the work inside each step runs across the warp's lanes.
  *
  *   child pair tests  the two children of an expanded pair on the two
- *                     half-warps; lane j of a half evaluates C2ARectDist's
- *                     edge-pair case j (rect_cases.cuh), the first case that
- *                     holds wins (ballot), else the face-separation tail;
- *                     then d = max(dist - r1 - r2, 0) and the motion bounds
+ *                     half-warps: the child transform one output per lane;
+ *                     C2ARectDist's shared sums a few per lane into
+ *                     shared-memory slots, lane j then tests edge-pair case j
+ *                     with operands read through tables (rect_table.cuh), the
+ *                     first case that holds wins (ballot) and only its lane
+ *                     evaluates the distance, else the face-separation tail;
+ *                     then d = max(dist - r1 - r2, 0) and the motion bounds,
+ *                     S one row per lane and the two bounds on alternate lanes
  *                     (C2A.cpp:1237-1274);
  *   TriDist           the nine segment pairs on nine lanes, then the
  *                     reference's in-order minimum/early-return logic replayed
  *                     over their results, and both vertex-over-face tests on
  *                     two lanes (C2A.cpp:165-405);
- *   control           descend decisions, the stack of pending second children
- *                     (shared memory, with their exact transforms) and the CA
- *                     loop run on every lane with identical values.
+ *   control           descend decisions and the CA loop run on every lane with
+ *                     identical values; the query state, the children just
+ *                     tested and the stack of pending second children (with
+ *                     their exact transforms) live in the warp's shared memory.
  *
  * Everything is the reference's FP64 arithmetic in its own order, so the
  * results are bit-identical to the thread-per-query kernel's (and the
