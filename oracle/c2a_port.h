@@ -27,6 +27,8 @@ typedef struct c2a_port_node {
     double r;           /* swept-sphere radius */
     double angR;        /* max vertex distance from the model origin */
     double Rloc[3][3];  /* build-time orientation in the model frame */
+    double To[3];       /* OBB centre, parent-relative (the static collide query) */
+    double d[3];        /* OBB half extents */
     int first_child;    /* >= 0 child index; < 0: -(triangle)-1 */
     int pad;
 } c2a_port_node;
@@ -84,6 +86,13 @@ double c2a_port_distance(const c2a_port_model *A, const c2a_port_model *B, const
 int c2a_port_tolerance(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
                        double tolerance, double *distance, double p1[3], double p2[3], long long *nbv,
                        long long *ntri);
+
+/* C2A_Collide (the PQP_CollideResult form, C2A_PQP.cpp:798-968) with B placed
+ * in A's frame by (R, T); flag 1 all contacts, 2 the first only.  Writes up
+ * to cap (id_a, id_b) caller-id pairs in the order found; returns the
+ * number of pairs found. */
+int c2a_port_collide(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
+                     int flag, int *pairs, int cap, long long *nbv, long long *ntri);
 
 typedef struct c2a_port_contact {
     int type_a, type_b;  /* 1 vertex, 2 edge, 3 face (C2A.cpp:1584-1585) */

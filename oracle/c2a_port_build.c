@@ -166,6 +166,26 @@ static void fit_rss(c2a_port_node *b, const double O[3][3], const c2a_port_tri *
 #define PX(k) P[3 * (k) + 0]
 #define PY(k) P[3 * (k) + 1]
 #define PZ(k) P[3 * (k) + 2]
+    /* the OBB in the same frame (C2A/src/C2A_BV.cpp:144-170): the projected
+     * extents, centre back in the model frame */
+    minx = maxx = PX(0);
+    miny = maxy = PY(0);
+    minz = maxz = PZ(0);
+    for (i = 1; i < np; i++) {
+        if (PX(i) < minx) minx = PX(i);
+        else if (PX(i) > maxx) maxx = PX(i);
+        if (PY(i) < miny) miny = PY(i);
+        else if (PY(i) > maxy) maxy = PY(i);
+        if (PZ(i) < minz) minz = PZ(i);
+        else if (PZ(i) > maxz) maxz = PZ(i);
+    }
+    c[0] = 0.5 * (maxx + minx);
+    c[1] = 0.5 * (maxy + miny);
+    c[2] = 0.5 * (maxz + minz);
+    pm_mul_v(b->To, (const double(*)[3])b->R, c);
+    b->d[0] = 0.5 * (maxx - minx);
+    b->d[1] = 0.5 * (maxy - miny);
+    b->d[2] = 0.5 * (maxz - minz);
     /* thickness -> radius and rectangle height */
     minz = maxz = PZ(0);
     for (i = 1; i < np; i++) {
@@ -334,18 +354,21 @@ static void build_recurse(build_ctx *ctx, int bn, int first_tri, int n)
 }
 
 /* C2A_Build.cpp:493-544 make_parent_relative (children first, then self) */
-static void make_parent_relative(c2a_port_model *m, int bn, const double pR[3][3], const double pTr[3])
+static void make_parent_relative(c2a_port_model *m, int bn, const double pR[3][3], const double pTr[3],
+                                 const double pTo[3])
 {
     c2a_port_node *b = &m->nodes[bn];
     double Rpc[3][3], Tpc[3];
     if (b->first_child >= 0) {
-        make_parent_relative(m, b->first_child, (const double(*)[3])b->R, b->Tr);
-        make_parent_relative(m, b->first_child + 1, (const double(*)[3])b->R, b->Tr);
+        make_parent_relative(m, b->first_child, (const double(*)[3])b->R, b->Tr, b->To);
+        make_parent_relative(m, b->first_child + 1, (const double(*)[3])b->R, b->Tr, b->To);
     }
     pm_tmul(Rpc, pR, (const double(*)[3])b->R);
     pm_copy(b->R, (const double(*)[3])Rpc);
     pv_sub(Tpc, b->Tr, pTr);
     pm_tmul_v(b->Tr, pR, Tpc);
+    pv_sub(Tpc, b->To, pTo);
+    pm_tmul_v(b->To, pR, Tpc);
 }
 
 int c2a_port_model_build(c2a_port_model *m, int num_tris, const double *tv, const int *ids, const int *vidx)
@@ -379,7 +402,7 @@ int c2a_port_model_build(c2a_port_model *m, int num_tris, const double *tv, cons
     ctx.m = m;
     ctx.num_nodes = 1;
     build_recurse(&ctx, 0, 0, num_tris);
-    make_parent_relative(m, 0, (const double(*)[3])I, Z);
+    make_parent_relative(m, 0, (const double(*)[3])I, Z, Z);
     free(ctx.P);
     return 0;
 }

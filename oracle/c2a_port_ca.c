@@ -509,6 +509,123 @@ int c2a_port_tolerance(const c2a_port_model *A, const c2a_port_model *B, const d
     return ts.closer;
 }
 
+/* --------------------------------------------------------- collide query */
+
+/* the OBB separating-axis test of the PQP interface as the oracle's shim
+ * states it (oracle/pqp_shim/pqp_shim.cpp): box b placed by (B, T) in box a's
+ * frame, the 15 axes with |B| inflated by 1e-6; 0 when no axis separates */
+static int obb_disjoint(const double B[3][3], const double T[3], const double a[3], const double b[3])
+{
+    double Bf[3][3], s, tproj, ra, rb;
+    int i, j;
+    for (i = 0; i < 3; i++)
+        for (j = 0; j < 3; j++) Bf[i][j] = fabs(B[i][j]) + 1e-6;
+    for (i = 0; i < 3; i++) {
+        s = b[0] * Bf[i][0] + b[1] * Bf[i][1] + b[2] * Bf[i][2];
+        if (fabs(T[i]) > a[i] + s) return 1;
+    }
+    for (j = 0; j < 3; j++) {
+        tproj = T[0] * B[0][j] + T[1] * B[1][j] + T[2] * B[2][j];
+        s = a[0] * Bf[0][j] + a[1] * Bf[1][j] + a[2] * Bf[2][j];
+        if (fabs(tproj) > b[j] + s) return 1;
+    }
+    for (i = 0; i < 3; i++) {
+        int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+        for (j = 0; j < 3; j++) {
+            int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+            tproj = T[i2] * B[i1][j] - T[i1] * B[i2][j];
+            ra = a[i1] * Bf[i2][j] + a[i2] * Bf[i1][j];
+            rb = b[j1] * Bf[i][j2] + b[j2] * Bf[i][j1];
+            if (fabs(tproj) > ra + rb) return 2;
+        }
+    }
+    return 0;
+}
+
+typedef struct coll_state {
+    const c2a_port_model *o1, *o2;
+    double R[3][3], T[3]; /* model 2 relative to model 1 */
+    int flag, num_pairs, cap;
+    int *pairs;
+    long long num_bv_tests, num_tri_tests;
+} coll_state;
+
+/* CollideRecurse, C2A/src/C2A_PQP.cpp:798-909: overlapping OBB pairs only,
+ * the first child before the second; triangles touch when their distance is
+ * zero (the shim's TriContact) */
+static void coll_recurse(coll_state *cs, const double R[3][3], const double T[3], int b1, int b2)
+{
+    const c2a_port_node *n1 = &cs->o1->nodes[b1], *n2 = &cs->o2->nodes[b2];
+    int l1 = n1->first_child < 0, l2 = n2->first_child < 0;
+    double Rc[3][3], Tc[3], Ttemp[3];
+    cs->num_bv_tests++;
+    if (obb_disjoint(R, T, n1->d, n2->d) != 0) return;
+    if (l1 && l2) {
+        const c2a_port_tri *t1 = &cs->o1->tris[-n1->first_child - 1], *t2 = &cs->o2->tris[-n2->first_child - 1];
+        double p[3], q[3];
+        cs->num_tri_tests++;
+        if (tri_distance_plain((const double(*)[3])cs->R, cs->T, t1, t2, p, q) == 0.0) {
+            if (cs->pairs && cs->num_pairs < cs->cap) {
+                cs->pairs[2 * cs->num_pairs] = t1->id;
+                cs->pairs[2 * cs->num_pairs + 1] = t2->id;
+            }
+            cs->num_pairs++;
+        }
+        return;
+    }
+    if (l2 || (!l1 && (node_size(n1) > node_size(n2)))) {
+        int c1 = n1->first_child, c2 = c1 + 1;
+        const c2a_port_node *m1 = &cs->o1->nodes[c1], *m2 = &cs->o1->nodes[c2];
+        pm_tmul(Rc, (const double(*)[3])m1->R, R);
+        pv_sub(Ttemp, T, m1->To);
+        pm_tmul_v(Tc, (const double(*)[3])m1->R, Ttemp);
+        coll_recurse(cs, (const double(*)[3])Rc, Tc, c1, b2);
+        if (cs->flag == 2 && cs->num_pairs > 0) return;
+        pm_tmul(Rc, (const double(*)[3])m2->R, R);
+        pv_sub(Ttemp, T, m2->To);
+        pm_tmul_v(Tc, (const double(*)[3])m2->R, Ttemp);
+        coll_recurse(cs, (const double(*)[3])Rc, Tc, c2, b2);
+    } else {
+        int c1 = n2->first_child, c2 = c1 + 1;
+        const c2a_port_node *m1 = &cs->o2->nodes[c1], *m2 = &cs->o2->nodes[c2];
+        pm_mul(Rc, R, (const double(*)[3])m1->R);
+        pm_mul_v_add(Tc, R, m1->To, T);
+        coll_recurse(cs, (const double(*)[3])Rc, Tc, b1, c1);
+        if (cs->flag == 2 && cs->num_pairs > 0) return;
+        pm_mul(Rc, R, (const double(*)[3])m2->R);
+        pm_mul_v_add(Tc, R, m2->To, T);
+        coll_recurse(cs, (const double(*)[3])Rc, Tc, b1, c2);
+    }
+}
+
+/* C2A_Collide (C2A_PQP.cpp:910-968): the root OBB pair's transform, then the recursion */
+int c2a_port_collide(const c2a_port_model *A, const c2a_port_model *B, const double R[9], const double T[3],
+                     int flag, int *pairs, int cap, long long *nbv, long long *ntri)
+{
+    coll_state cs;
+    double Rm[3][3], Rtemp[3][3], Rr[3][3], Ttemp[3], Tr[3];
+    const c2a_port_node *r1 = &A->nodes[0], *r2 = &B->nodes[0];
+    pm_from9(Rm, R);
+    cs.o1 = A;
+    cs.o2 = B;
+    pm_copy(cs.R, (const double(*)[3])Rm);
+    pv_copy(cs.T, T);
+    cs.flag = flag;
+    cs.num_pairs = 0;
+    cs.cap = cap;
+    cs.pairs = pairs;
+    cs.num_bv_tests = cs.num_tri_tests = 0;
+    pm_mul(Rtemp, (const double(*)[3])Rm, (const double(*)[3])r2->R);
+    pm_tmul(Rr, (const double(*)[3])r1->R, (const double(*)[3])Rtemp);
+    pm_mul_v_add(Ttemp, (const double(*)[3])Rm, r2->To, T);
+    pv_sub(Ttemp, Ttemp, r1->To);
+    pm_tmul_v(Tr, (const double(*)[3])r1->R, Ttemp);
+    coll_recurse(&cs, (const double(*)[3])Rr, Tr, 0, 0);
+    if (nbv) *nbv = cs.num_bv_tests;
+    if (ntri) *ntri = cs.num_tri_tests;
+    return cs.num_pairs;
+}
+
 /* -------------------------------------------------- translation-only CA */
 
 /* CInterpMotion_Linear::CAonNonAdjacentTriangles, InterpMotion.cpp:657-743 */

@@ -55,6 +55,7 @@ class _PortModel(C.Structure):
 
 NODE_DTYPE = np.dtype([("R", np.float64, (9,)), ("Tr", np.float64, (3,)), ("l", np.float64, (2,)),
                        ("r", np.float64), ("angR", np.float64), ("Rloc", np.float64, (9,)),
+                       ("To", np.float64, (3,)), ("d", np.float64, (3,)),
                        ("first_child", np.int32), ("pad", np.int32)], align=True)
 TRI_DTYPE = np.dtype([("v", np.float64, (9,)), ("id", np.int32), ("idx", np.int32, (3,))], align=True)
 
@@ -95,6 +96,9 @@ class Port:
         L.c2a_port_tolerance.argtypes = [C.POINTER(_PortModel), C.POINTER(_PortModel), C.c_void_p, C.c_void_p,
                                          C.c_double] + [C.c_void_p] * 5
         L.c2a_port_tolerance.restype = C.c_int
+        L.c2a_port_collide.argtypes = [C.POINTER(_PortModel), C.POINTER(_PortModel), C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.c2a_port_collide.restype = C.c_int
 
     def models(self, meshes) -> C.Array:
         """Builds every mesh's hierarchy; returns a ctypes array of models."""
@@ -149,6 +153,16 @@ class Port:
                                         _dptr(d), _dptr(p1), _dptr(p2), _dptr(n[0:1]), _dptr(n[1:2]))
         return c, float(d[0]), p1, p2, int(n[0]), int(n[1])
 
+    def collide(self, models, ia: int, ib: int, R, T, flag: int = 1, cap: int = 1 << 16):
+        """C2A_Collide: (pairs (k, 2) caller ids in the order found, num_bv_tests, num_tri_tests)."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(9)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(3)
+        pairs = np.zeros((cap, 2), dtype=np.int32)
+        n = np.zeros(2, dtype=np.int64)
+        k = self.lib.c2a_port_collide(C.byref(models[ia]), C.byref(models[ib]), _dptr(R), _dptr(T), int(flag),
+                                      _dptr(pairs), cap, _dptr(n[0:1]), _dptr(n[1:2]))
+        return pairs[:min(k, cap)].copy(), int(n[0]), int(n[1])
+
     def rectdist(self, Rab, Tab, a, b):
         Rab = np.ascontiguousarray(Rab, dtype=np.float64).reshape(9)
         Tab, a, b = (np.ascontiguousarray(x, dtype=np.float64) for x in (Tab, a, b))
@@ -194,6 +208,8 @@ class Ref:
         L.c2a_ref_distance.restype = C.c_double
         L.c2a_ref_tolerance.argtypes = [C.c_void_p] * 4 + [C.c_double, C.c_void_p]
         L.c2a_ref_tolerance.restype = C.c_int
+        L.c2a_ref_collide.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p, C.c_int, C.c_void_p]
+        L.c2a_ref_collide.restype = C.c_int
 
     @staticmethod
     def available() -> bool:
@@ -269,6 +285,15 @@ class Ref:
         out = np.zeros(9)
         c = self.lib.c2a_ref_tolerance(ha, hb, _dptr(R), _dptr(T), float(tol), _dptr(out))
         return c, float(out[0]), out[1:4].copy(), out[4:7].copy(), int(out[7]), int(out[8])
+
+    def collide(self, ha, hb, R, T, flag: int = 1, cap: int = 1 << 16):
+        """The reference's C2A_Collide: (pairs (k, 2) caller ids in order, num_bv_tests, num_tri_tests)."""
+        R = np.ascontiguousarray(R, dtype=np.float64).reshape(9)
+        T = np.ascontiguousarray(T, dtype=np.float64).reshape(3)
+        pairs = np.zeros((cap, 2), dtype=np.int32)
+        n = np.zeros(2, dtype=np.int64)
+        k = self.lib.c2a_ref_collide(ha, hb, _dptr(R), _dptr(T), int(flag), _dptr(pairs), cap, _dptr(n))
+        return pairs[:min(k, cap)].copy(), int(n[0]), int(n[1])
 
     def motion(self, R0, T0, R1, T1, t):
         args = [np.ascontiguousarray(x, dtype=np.float64).reshape(-1) for x in (R0, T0, R1, T1)]

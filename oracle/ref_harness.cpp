@@ -233,6 +233,27 @@ int c2a_ref_tolerance(void *ha, void *hb, const double *R9, const double *T3, do
   return res.closer_than_tolerance;
 }
 
+// C2A_Collide (the PQP_CollideResult form); R/T place model B in model A's
+// frame.  Writes up to cap (id1, id2) pairs; counts[0..1]: BV and triangle
+// tests; returns the number of pairs.
+int c2a_ref_collide(void *ha, void *hb, const double *R9, const double *T3, int flag, int *pairs, int cap,
+                    long long *counts)
+{
+  C2A_Model *A = (C2A_Model *)ha, *B = (C2A_Model *)hb;
+  PQP_REAL I[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, Z[3] = {0, 0, 0}, R[3][3], T[3];
+  m9(R, R9);
+  VcV(T, T3);
+  PQP_CollideResult res;
+  C2A_Collide(&res, I, Z, A, R, T, B, flag);
+  for (int k = 0; k < res.num_pairs && k < cap; k++) {
+    pairs[2 * k] = res.Id1(k);
+    pairs[2 * k + 1] = res.Id2(k);
+  }
+  counts[0] = res.num_bv_tests;
+  counts[1] = res.num_tri_tests;
+  return res.num_pairs;
+}
+
 // C2A_Distance (rel_err = abs_err = 0, qsize 2) from a seed pair; R/T place
 // model B in model A's frame.  Returns the distance; *ta/*tb the closest pair.
 double c2a_ref_distance(void *ha, void *hb, const double *R9, const double *T3, int seed_a, int seed_b, int *ta,

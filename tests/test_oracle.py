@@ -148,3 +148,33 @@ def test_port_tolerance_matches_reference(port, ref):
             found += 1
             assert bits(got[1]) == bits(exp[1]) and bits(got[2]) == bits(exp[2]) and bits(got[3]) == bits(exp[3]), k
     assert 30 < found < 120
+
+
+def test_port_collide_matches_reference(port, ref):
+    """C2A_Collide (the PQP_CollideResult form, C2A/src/C2A_PQP.cpp:798-968):
+    the port against the compiled reference, both with every contact and
+    with the first only -- the colliding triangle-id pairs in the order
+    found and the BV/triangle counters, exactly.  The hierarchy's OBB fields
+    (C2A_BV.cpp:144-170, make_parent_relative) come from the port's build."""
+    from c2a_gb300 import meshes, workloads
+
+    ms = [meshes.torus_knot(2, 3, 40, 8), meshes.triangle_soup(600, clusters=5, seed=81),
+          meshes.icosphere(2, radius=0.8, noise=0.02, seed=82)]
+    models = port.models(ms)
+    ha = [ref.model(m) for m in ms]
+    hb = [ref.model(m) for m in ms]
+    rng = np.random.default_rng(83)
+    hits = 0
+    for k in range(80):
+        a, b = rng.integers(0, 3, 2)
+        R = workloads.random_rotations(rng, 1).reshape(9)
+        T = workloads.unit_vectors(rng, 1)[0] * rng.uniform(0.0, 1.6) + rng.normal(scale=1e-3, size=3)
+        for flag in (1, 2):
+            got = port.collide(models, a, b, R, T, flag)
+            exp = ref.collide(ha[a], hb[b], R, T, flag)
+            assert np.array_equal(got[0], exp[0]) and got[1:] == exp[1:], (k, flag, len(got[0]), len(exp[0]),
+                                                                          got[1:], exp[1:])
+            if flag == 1 and len(exp[0]):
+                hits += 1
+                assert len(port.collide(models, a, b, R, T, 2)[0]) == 1
+    assert 15 < hits < 80, hits
