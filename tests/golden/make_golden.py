@@ -258,9 +258,45 @@ def distance_fixtures(ref):
     np.savez_compressed(os.path.join(HERE, "distance_ref.npz"), **arrays)
 
 
+def static_query_fixtures(ref):
+    """C2A_Tolerance (qsize 2) and C2A_Collide (every contact) of the reference
+    on a knot, a soup and an icosphere, placed from overlapping to apart."""
+    ms = [meshes.torus_knot(2, 3, 40, 8), meshes.triangle_soup(600, clusters=5, seed=91),
+          meshes.icosphere(2, radius=0.8, noise=0.02, seed=92)]
+    with quiet_stdout():
+        ha = [ref.model(m) for m in ms]
+        hb = [ref.model(m) for m in ms]
+    rng = np.random.default_rng(93)
+    n = 96
+    ab = rng.integers(0, 3, (n, 2)).astype(np.int32)
+    R = workloads.random_rotations(rng, n).reshape(n, 9)
+    T = workloads.unit_vectors(rng, n) * rng.uniform(0.0, 2.0, (n, 1)) + rng.normal(scale=1e-3, size=(n, 3))
+    tol = rng.uniform(0.0, 0.3, n)
+    closer = np.zeros(n, np.int32)
+    tol_out = np.zeros((n, 9))
+    pairs, offs, ccount = [], [0], np.zeros((n, 2), np.int64)
+    for i, (a, b) in enumerate(ab):
+        c, d, p1, p2, nbv, ntri = ref.tolerance(ha[a], hb[b], R[i], T[i], tol[i])
+        closer[i] = c
+        tol_out[i] = [d, *p1, *p2, nbv, ntri]
+        pr, cbv, ctri = ref.collide(ha[a], hb[b], R[i], T[i], 1)
+        pairs.append(pr)
+        offs.append(offs[-1] + len(pr))
+        ccount[i] = [cbv, ctri]
+    arrays = dict(num_meshes=len(ms), ab=ab, R=R, T=T, tol=tol, closer=closer, tol_out=tol_out,
+                  pairs=np.concatenate(pairs).astype(np.int32), pair_offsets=np.array(offs), collide_counts=ccount)
+    for i, m in enumerate(ms):
+        arrays[f"mesh{i}_verts"] = m.verts
+        arrays[f"mesh{i}_faces"] = m.faces
+    np.savez_compressed(os.path.join(HERE, "static_queries_ref.npz"), **arrays)
+
+
 def main():
     build(ref=True)
     ref = Ref()
+    if sys.argv[1:] == ["static"]:
+        static_query_fixtures(ref)
+        return
     if sys.argv[1:] == ["canonical"]:
         canonical_fixtures(ref)
         return
@@ -309,6 +345,7 @@ def main():
     bvh_hashes(ref)
     canonical_fixtures(ref)
     distance_fixtures(ref)
+    static_query_fixtures(ref)
 
 
 if __name__ == "__main__":

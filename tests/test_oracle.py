@@ -178,3 +178,25 @@ def test_port_collide_matches_reference(port, ref):
                 hits += 1
                 assert len(port.collide(models, a, b, R, T, 2)[0]) == 1
     assert 15 < hits < 80, hits
+
+
+def test_port_static_queries_match_reference_fixture(port):
+    """C2A_Tolerance and C2A_Collide of the port against the reference's own
+    outputs stored in tests/golden/static_queries_ref.npz (runs where the
+    reference sources are absent)."""
+    from c2a_gb300 import meshes
+
+    z = np.load(f"{GOLDEN}/static_queries_ref.npz")
+    ms = [meshes.Mesh(f"s{i}", z[f"mesh{i}_verts"], z[f"mesh{i}_faces"], np.zeros((1, 3)), 0.0)
+          for i in range(int(z["num_meshes"]))]
+    models = port.models(ms)
+    offs = z["pair_offsets"]
+    for i, (a, b) in enumerate(z["ab"]):
+        c, d, p1, p2, nbv, ntri = port.tolerance(models, a, b, z["R"][i], z["T"][i], z["tol"][i])
+        e = z["tol_out"][i]
+        assert c == z["closer"][i] and (nbv, ntri) == (int(e[7]), int(e[8])), i
+        if c:
+            assert bits(d) == bits(e[0]) and bits(p1) == bits(e[1:4]) and bits(p2) == bits(e[4:7]), i
+        pairs, cbv, ctri = port.collide(models, a, b, z["R"][i], z["T"][i], 1)
+        assert np.array_equal(pairs, z["pairs"][offs[i]:offs[i + 1]]), i
+        assert (cbv, ctri) == tuple(z["collide_counts"][i]), i
