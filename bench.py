@@ -60,7 +60,7 @@ def parse():
                         "CANONICAL batches on held-out queries")
     p.add_argument("--train", type=int, default=262144, help="--mode learned: training queries")
     p.add_argument("--epochs", type=int, default=6, help="--mode learned: training epochs")
-    p.add_argument("--engine", choices=["auto", "warp", "thread", "batched"], default="auto")
+    p.add_argument("--engine", choices=["auto", "warp", "thread", "batched", "spec"], default="auto")
     p.add_argument("--order", choices=["learned", "geometric"], default="learned",
                    help="REFERENCE mode: the work-queue order; learned: a cost model trained on another seed's "
                         "queries (costs measured by the library) starts the costliest queries first; geometric: "
@@ -195,8 +195,9 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-ENGINES = {"auto": 0, "warp": 1, "batched": 2, "thread": 3}
+ENGINES = {"auto": 0, "warp": 1, "batched": 2, "thread": 3, "spec": 4}
 KERNELS = {("reference", "auto"): "c2a_solve_warp_kernel", ("reference", "warp"): "c2a_solve_warp_kernel",
+           ("reference", "spec"): "c2a_solve_spec_kernel",
            ("reference", "thread"): "c2a_solve_kernel", ("canonical", "auto"): "c2a_canonical_kernel",
            ("canonical", "warp"): "c2a_canonical_kernel", ("canonical", "batched"): "k_dsearch"}
 

@@ -35,6 +35,9 @@ assert DISTANCE_DTYPE.itemsize == 72
 
 C2A_OK = 0
 QUERY_BAD_INPUT, QUERY_STACK_OVERFLOW, QUERY_CONTACT_OVERFLOW, QUERY_ITER_CAP = 1, 2, 4, 8
+(OK, ERR_INVALID_ARGUMENT, ERR_NO_DEVICE, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_EMPTY_MODEL, ERR_BAD_MODEL,
+ ERR_TREE_TOO_DEEP, ERR_QUERY_FAILED, ERR_NOALLOC_CAPACITY) = range(10)
+NOALLOC_MAX_MODELS = 120  # C2A_NOALLOC_MAX_MODELS
 
 # every extern "C" symbol of include/c2a_gb300.h
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
@@ -53,7 +56,7 @@ class Params(C.Structure):
 
 
 MODE_REFERENCE, MODE_CANONICAL = 0, 1
-ENGINE_AUTO, ENGINE_WARP, ENGINE_BATCHED, ENGINE_THREAD = 0, 1, 2, 3
+ENGINE_AUTO, ENGINE_WARP, ENGINE_BATCHED, ENGINE_THREAD, ENGINE_SPEC = 0, 1, 2, 3, 4
 
 
 class Contacts:

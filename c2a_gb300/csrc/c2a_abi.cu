@@ -8,13 +8,16 @@
 
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <new>
 #include <vector>
 
 #include "../../include/c2a_gb300.h"
 #include "device/ca_front.cuh"
+#include "device/ca_spec.cuh"
 #include "device/ca_warp.cuh"
+#include "kernels.h"
 #include "host/bvh_build.h"
 #include "wave_engine.h"
 
@@ -22,7 +25,7 @@ using namespace c2a;
 
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = kBlockThreads;
 
 struct ModelSlot {
     BuiltModel host;
@@ -87,6 +90,13 @@ struct c2a_context {
     int warp_cap = 0;            /* the warp kernel's stack entries the occupancy above was computed for */
     bool warp_smem_attr = false;
     int distance_blocks_per_sm = 0;
+    /* the speculative engine: occupancy for (stack cap, records), FP64 record scratch */
+    int spec_blocks_per_sm = 0;
+    int spec_cap = 0, spec_nrec = 0;
+    bool spec_smem_attr = false;
+    unsigned char *d_spec = nullptr;
+    size_t spec_bytes = 0;
+    uint64_t models_gen = 0;     /* changes whenever a model is built or freed (unique across contexts) */
     std::mutex mu;
 };
 
@@ -161,8 +171,8 @@ bool params_ok(const c2a_params *p)
 {
     return p && p->max_iters >= 0 && p->contacts_per_query >= 0 &&
            (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL) && p->engine >= C2A_ENGINE_AUTO &&
-           p->engine <= C2A_ENGINE_THREAD && !(p->mode == C2A_MODE_REFERENCE && p->engine == C2A_ENGINE_BATCHED) &&
-           !(p->mode == C2A_MODE_CANONICAL && p->engine == C2A_ENGINE_THREAD);
+           p->engine <= C2A_ENGINE_SPEC && !(p->mode == C2A_MODE_REFERENCE && p->engine == C2A_ENGINE_BATCHED) &&
+           !(p->mode == C2A_MODE_CANONICAL && (p->engine == C2A_ENGINE_THREAD || p->engine == C2A_ENGINE_SPEC));
 }
 
 /* queries must not pair models deeper than the traversal stack */
@@ -196,244 +206,6 @@ Shape shape_for(c2a_context *ctx, int n)
 
 /* ------------------------------------------------------------- kernels */
 
-__global__ void __launch_bounds__(kThreads) c2a_solve_kernel(const c2a_query *__restrict__ queries, int n,
-                                                             const DevModel *__restrict__ models, int num_models,
-                                                             c2a_params prm, c2a_result *__restrict__ results,
-                                                             c2a_contact *__restrict__ contacts,
-                                                             unsigned int *__restrict__ counter)
-{
-    Pending stack[C2A_STACK_DEPTH];
-    for (;;) {
-        const unsigned int q = atomicAdd(counter, 1u);
-        if (q >= (unsigned int)n) break;
-        c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
-        solve_query(queries[q], models, num_models, prm, results[q], cq, stack, (int)q);
-    }
-}
-
-__global__ void __launch_bounds__(kThreads) c2a_step_kernel(const c2a_query *__restrict__ queries, int n,
-                                                            const double *__restrict__ lambda,
-                                                            const int32_t *__restrict__ num_ca,
-                                                            const double *__restrict__ prev_mint,
-                                                            const DevModel *__restrict__ models, int num_models,
-                                                            c2a_params prm, c2a_result *__restrict__ results)
-{
-    Pending stack[C2A_STACK_DEPTH];
-    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= n) return;
-    const c2a_query &in = queries[qi];
-    c2a_result &out = results[qi];
-    out.status = 0;
-    if (in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 || in.model_b >= num_models ||
-        !(models[in.model_a].flags & C2A_MODEL_LIVE) || !(models[in.model_b].flags & C2A_MODEL_LIVE)) {
-        out.status = C2A_QUERY_BAD_INPUT;
-        return;
-    }
-    Query q;
-    q.A = models + in.model_a;
-    q.B = models + in.model_b;
-    q.want_mint = true;
-    if (in.seed_a < 0 || in.seed_a >= q.A->num_tris || in.seed_b < 0 || in.seed_b >= q.B->num_tris) {
-        out.status = C2A_QUERY_BAD_INPUT;
-        return;
-    }
-    q.status = 0;
-    const double *P = in.pose;
-    set_motions(q, P);
-    q.toc_delta = prm.toc_delta;
-    const bool translation = (q.m1.angVel < 1e-8 && q.m2.angVel < 1e-8);
-    const double lam = lambda[qi];
-    M3 R1, R2;
-    V3 T1, T2;
-    if (lam == 0.0) {
-        R1 = pose_R(P);
-        T1 = pose_T(P);
-        R2 = pose_R(P + 24);
-        T2 = pose_T(P + 24);
-    } else {
-        double orn[4];
-        motion_integrate(q.m1, lam, R1.m, &T1.x, orn);
-        motion_integrate(q.m2, lam, R2.m, &T2.x, orn);
-    }
-    set_pose1(q, R1, T1);
-    q.seed_a = in.seed_a;
-    q.seed_b = in.seed_b;
-    q.nbv = q.ntri = 0;
-    q.numCA = num_ca[qi];
-    q.mint = prev_mint[qi];
-    q.upbound = 1.0 - lam;
-    q.distance = 0;
-    q.abs_err = q.rel_err = 0;
-    toc_step(q, R1, T1, R2, T2, translation, stack);
-    out.collisionfree = 0;
-    out.numCA = q.numCA;
-    out.translation = translation ? 1 : 0;
-    out.num_contact = 0;
-    out.toc = lam;
-    out.distance = q.distance;
-    out.mint = q.mint;
-    out.num_bv_tests = q.nbv;
-    out.num_tri_tests = q.ntri;
-    out.seed_a = q.seed_a;
-    out.seed_b = q.seed_b;
-    out.status = q.status;
-}
-
-__global__ void __launch_bounds__(kThreads) c2a_contact_kernel(const c2a_query *__restrict__ queries, int n,
-                                                               const double *__restrict__ threshold,
-                                                               const DevModel *__restrict__ models, int num_models,
-                                                               int slots, c2a_result *__restrict__ results,
-                                                               c2a_contact *__restrict__ contacts)
-{
-    Pending stack[C2A_STACK_DEPTH];
-    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qi >= n) return;
-    const c2a_query &in = queries[qi];
-    c2a_result &out = results[qi];
-    out.status = 0;
-    out.num_contact = 0;
-    if (in.model_a < 0 || in.model_a >= num_models || in.model_b < 0 || in.model_b >= num_models ||
-        !(models[in.model_a].flags & C2A_MODEL_LIVE) || !(models[in.model_b].flags & C2A_MODEL_LIVE)) {
-        out.status = C2A_QUERY_BAD_INPUT;
-        return;
-    }
-    Query q;
-    q.A = models + in.model_a;
-    q.B = models + in.model_b;
-    q.status = 0;
-    q.want_mint = false; /* the contact recursion reads distances only */
-    q.e_ok = true;
-    q.nbv = q.ntri = 0;
-    const double *P = in.pose;
-    M3 R;
-    V3 T;
-    relative_transforms(q, pose_R(P), pose_T(P), pose_R(P + 24), pose_T(P + 24), R, T);
-    q.shadows_ok = q.e_ok && ((q.A->flags & q.B->flags) & C2A_MODEL_SHADOW_OK);
-    const int cnt = contact_dfs(q, R, T, threshold[qi], stack,
-                                contacts ? contacts + (size_t)qi * (size_t)slots : nullptr, slots, qi);
-    out.num_contact = cnt;
-    out.contact_offset = qi * slots;
-    out.status = q.status | (cnt > slots ? C2A_QUERY_CONTACT_OVERFLOW : 0);
-}
-
-/* The order warps take queries in: queries whose bounding spheres close in on
- * each other over the motion go first (they run many CA iterations), the
- * rest after, so the longest queries do not start last.  Results are written
- * by query index; the order changes nothing else. */
-__global__ void c2a_schedule_kernel(const c2a_query *__restrict__ queries, int n,
-                                    const DevModel *__restrict__ models, int num_models,
-                                    int32_t *__restrict__ order, unsigned int *__restrict__ ends)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const c2a_query &q = queries[i];
-    bool early = false;
-    if (q.model_a >= 0 && q.model_a < num_models && q.model_b >= 0 && q.model_b < num_models &&
-        (models[q.model_a].flags & C2A_MODEL_LIVE) && (models[q.model_b].flags & C2A_MODEL_LIVE)) {
-        const NodeRec *ra = models[q.model_a].nodes, *rb = models[q.model_b].nodes;
-        /* root rectangle centres and bounding radii in each model's frame */
-        const V3 ca = mul(load_R(ra), v3(0.5 * ra->l[0], 0.5 * ra->l[1], 0.0)) + load_Tr(ra);
-        const V3 cb = mul(load_R(rb), v3(0.5 * rb->l[0], 0.5 * rb->l[1], 0.0)) + load_Tr(rb);
-        const double rad = 0.5 * (ra->size + rb->size);
-        const double *P = q.pose;
-        const V3 pa0 = mul(pose_R(P), ca) + pose_T(P), pb0 = mul(pose_R(P + 24), cb) + pose_T(P + 24);
-        const V3 pa1 = mul(pose_R(P + 12), ca) + pose_T(P + 12), pb1 = mul(pose_R(P + 36), cb) + pose_T(P + 36);
-        const V3 g0 = pb0 - pa0, g1 = pb1 - pa1;
-        /* the segment between the centres' relative start and end positions comes within reach */
-        const V3 dg = g1 - g0;
-        const double L2 = dot(dg, dg);
-        double t = L2 > 0 ? -dot(g0, dg) / L2 : 0.0;
-        t = t < 0 ? 0 : (t > 1 ? 1 : t);
-        const V3 gm = g0 + mul_s(dg, t);
-        early = dot(gm, gm) < rad * rad;
-    }
-    const unsigned int k = atomicAdd(ends + (early ? 0 : 1), 1u);
-    if (early) order[k] = i;
-    else order[n - 1 - (int)k] = i;
-}
-
-/* REFERENCE mode on one warp per query (persistent): the reference's order,
- * each node-pair test split across the lanes */
-#ifndef C2A_WARP_MINB
-#define C2A_WARP_MINB 1
-#endif
-__global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel(const c2a_query *__restrict__ queries, int n,
-                                                                  const DevModel *__restrict__ models,
-                                                                  int num_models, c2a_params prm,
-                                                                  c2a_result *__restrict__ results,
-                                                                  c2a_contact *__restrict__ contacts,
-                                                                  unsigned int *__restrict__ counter,
-                                                                  const int32_t *__restrict__ order, int stack_cap)
-{
-    extern __shared__ __align__(16) unsigned char c2a_warp_smem[];
-    Pending tstack[C2A_STACK_DEPTH]; /* the translation-only step's sequential stack */
-    const int lane = threadIdx.x & 31;
-    WarpShared &mine = *reinterpret_cast<WarpShared *>(c2a_warp_smem + (threadIdx.x >> 5) *
-                                                       warp_shared_bytes(stack_cap));
-    mine.cap = stack_cap;
-    for (;;) {
-        unsigned int q = 0;
-        if (lane == 0) q = atomicAdd(counter, 1u);
-        q = __shfl_sync(kFullMask, q, 0);
-        if (q >= (unsigned int)n) break;
-        if (order) {
-            const int32_t o = order[q];
-            if (o < 0 || o >= n) continue; /* not a valid query index: skipped */
-            q = (unsigned int)o;
-        }
-        c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
-        solve_query_warp(queries[q], models, num_models, prm, results[q], cq, mine, tstack, (int)q, lane);
-    }
-}
-
-/* CANONICAL mode: one warp per query (persistent; warps take queries from
- * the work counter), each with its own slice of the front buffer */
-__global__ void __launch_bounds__(kThreads) c2a_canonical_kernel(const c2a_query *__restrict__ queries, int n,
-                                                                 const DevModel *__restrict__ models,
-                                                                 int num_models, c2a_params prm,
-                                                                 c2a_result *__restrict__ results,
-                                                                 c2a_contact *__restrict__ contacts,
-                                                                 unsigned int *__restrict__ counter,
-                                                                 Pending *__restrict__ fronts,
-                                                                 const uint32_t *__restrict__ hints, int nh)
-{
-    const int lane = threadIdx.x & 31;
-    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    Pending *stack = fronts + warp * (size_t)C2A_FRONT_CAP;
-    for (;;) {
-        unsigned int q = 0;
-        if (lane == 0) q = atomicAdd(counter, 1u);
-        q = __shfl_sync(kFullMask, q, 0);
-        if (q >= (unsigned int)n) break;
-        c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
-        solve_query_canonical(queries[q], models, num_models, prm, results[q], cq, stack, C2A_FRONT_CAP, lane,
-                              (int)q, hints ? hints + (size_t)q * nh * 2 : nullptr, nh);
-    }
-}
-
-/* C2A_Distance for a batch: one warp per pair (persistent), each with its own
- * slice of the front buffer */
-__global__ void __launch_bounds__(kThreads) c2a_distance_kernel(const c2a_query *__restrict__ queries, int n,
-                                                                const DevModel *__restrict__ models, int num_models,
-                                                                c2a_distance_result *__restrict__ results,
-                                                                unsigned int *__restrict__ counter,
-                                                                Pending *__restrict__ fronts)
-{
-    const int lane = threadIdx.x & 31;
-    const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    Pending *stack = fronts + warp * (size_t)C2A_FRONT_CAP;
-    for (;;) {
-        unsigned int q = 0;
-        if (lane == 0) q = atomicAdd(counter, 1u);
-        q = __shfl_sync(kFullMask, q, 0);
-        if (q >= (unsigned int)n) break;
-        distance_query_warp(queries[q], models, num_models, results[q], stack, C2A_FRONT_CAP, lane);
-    }
-}
-
-/* dense contact output: exclusive scan of min(num_contact, slots), then a
- * gather of the used slots (one block per 1024 queries, block-local scan
- * followed by a scan of the block totals) */
 constexpr int kScanBlock = 1024;
 
 __global__ void __launch_bounds__(kScanBlock) c2a_scan_blocks(c2a_result *__restrict__ results, int n, int slots,
@@ -499,8 +271,13 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 unsigned char *g_noalloc_ptr[kMaxDevices] = {};
+uint64_t g_noalloc_table_gen[kMaxDevices] = {}; /* models_gen of the table last uploaded on each device */
+std::atomic<uint64_t> g_models_gen{0};
 
-/* device address of the scratch array on `device` (current), looked up once */
+uint64_t next_models_gen() { return ++g_models_gen; }
+
+/* device address of the scratch array on `device` (current), looked up once
+ * per device; c2a_create calls it, so the first query call finds it set */
 c2a_status noalloc_scratch(int device, unsigned char **out)
 {
     if (device < 0 || device >= kMaxDevices) return C2A_ERR_INVALID_ARGUMENT;
@@ -560,8 +337,19 @@ c2a_status c2a_create(int device, c2a_context **out)
     if (!ctx) return C2A_ERR_OUT_OF_MEMORY;
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    ctx->models_gen = next_models_gen();
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->d_counter, sizeof(unsigned int) * 4) != cudaSuccess) {
+        c2a_destroy(ctx);
+        return C2A_ERR_CUDA;
+    }
+    /* set-up of c2a_solve_batch_noalloc, done here because this call may
+     * allocate: the scratch array's device address on this device, and the
+     * module of its kernel loaded (lazy loading would otherwise load it, and
+     * reserve its local memory, on the first no-alloc call) */
+    unsigned char *scratch = nullptr;
+    cudaFuncAttributes fa;
+    if (noalloc_scratch(device, &scratch) != C2A_OK || cudaFuncGetAttributes(&fa, c2a_solve_kernel) != cudaSuccess) {
         c2a_destroy(ctx);
         return C2A_ERR_CUDA;
     }
@@ -582,6 +370,7 @@ c2a_status c2a_destroy(c2a_context *ctx)
     if (ctx->d_models) cudaFree(ctx->d_models);
     if (ctx->d_fronts) cudaFree(ctx->d_fronts);
     if (ctx->d_order) cudaFree(ctx->d_order);
+    if (ctx->d_spec) cudaFree(ctx->d_spec);
     wave_free(ctx->wave);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->d_buf) cudaFree(ctx->d_buf);
@@ -639,6 +428,7 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
     slot.live = true;
     ctx->models.push_back(std::move(slot));
     ctx->models_dirty = true;
+    ctx->models_gen = next_models_gen();
     *model_id = (int32_t)ctx->models.size() - 1;
     return C2A_OK;
 }
@@ -698,6 +488,7 @@ c2a_status c2a_model_free(c2a_context *ctx, int32_t id)
     s.live = false;
     s.host = BuiltModel();
     ctx->models_dirty = true;
+    ctx->models_gen = next_models_gen();
     return C2A_OK;
 }
 
@@ -718,7 +509,9 @@ c2a_status c2a_solve_batch_ordered(c2a_context *ctx, const c2a_query *d_queries,
                                    c2a_contact *d_contacts, void *stream)
 {
     if (!params || params->mode != C2A_MODE_REFERENCE ||
-        (params->engine != C2A_ENGINE_AUTO && params->engine != C2A_ENGINE_WARP) || (n > 0 && !d_order))
+        (params->engine != C2A_ENGINE_AUTO && params->engine != C2A_ENGINE_WARP &&
+         params->engine != C2A_ENGINE_SPEC) ||
+        (n > 0 && !d_order))
         return C2A_ERR_INVALID_ARGUMENT;
     return solve_device(ctx, d_queries, n, params, d_results, d_contacts, stream, nullptr, 0, d_order);
 }
@@ -773,6 +566,63 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
         return C2A_OK;
     }
     C2A_CUDA(cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned int), s));
+    if (prm.engine != C2A_ENGINE_THREAD && (size_t)n > ctx->order_cap) {
+        C2A_CUDA(cudaStreamSynchronize(s));
+        if (ctx->d_order) cudaFree(ctx->d_order);
+        ctx->d_order = nullptr;
+        ctx->order_cap = 0;
+        C2A_CUDA(cudaMalloc(&ctx->d_order, sizeof(int32_t) * (size_t)n));
+        ctx->order_cap = (size_t)n;
+    }
+    if (prm.engine == C2A_ENGINE_SPEC) {
+        /* the stack holds one pending pair per BVTT level: 2 depth + 2 entries;
+         * records: the replay's path (one per BVTT level) plus 64 for speculation */
+        const int cap = 2 * deepest + 2 > 4 ? 2 * deepest + 2 : 4;
+        const int nrec = 2 * deepest + 2 + 64;
+        const size_t per = warp_shared_bytes(cap) + spec_shared_bytes(nrec);
+        const size_t smem = per * (kThreads / 32);
+        if (!ctx->spec_smem_attr) {
+            int optin = 0;
+            C2A_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+            C2A_CUDA(cudaFuncSetAttribute(c2a_solve_spec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+            ctx->spec_smem_attr = true;
+        }
+        if (ctx->spec_cap != cap || ctx->spec_nrec != nrec) {
+            int occ = 0;
+            C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_solve_spec_kernel, kThreads, smem));
+            if (occ < 1) return C2A_ERR_TREE_TOO_DEEP; /* the per-warp state does not fit shared memory */
+            ctx->spec_blocks_per_sm = occ;
+            ctx->spec_cap = cap;
+            ctx->spec_nrec = nrec;
+        }
+        const int most = ctx->sm_count * ctx->spec_blocks_per_sm;
+        const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
+        const int blocks = need < most ? need : most;
+        const size_t gbytes = spec_global_bytes(nrec) * (size_t)blocks * (kThreads / 32);
+        if (gbytes > ctx->spec_bytes) {
+            C2A_CUDA(cudaStreamSynchronize(s));
+            if (ctx->d_spec) cudaFree(ctx->d_spec);
+            ctx->d_spec = nullptr;
+            ctx->spec_bytes = 0;
+            const size_t want = spec_global_bytes(nrec) * (size_t)most * (kThreads / 32);
+            C2A_CUDA(cudaMalloc(&ctx->d_spec, want > gbytes ? want : gbytes));
+            ctx->spec_bytes = want > gbytes ? want : gbytes;
+        }
+        if (!user_order) { /* queries whose bounding spheres approach go first */
+            C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 1, 0, 2 * sizeof(unsigned int), s));
+            c2a_schedule_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_queries, n, ctx->d_models,
+                                                                 (int)ctx->models.size(), ctx->d_order,
+                                                                 ctx->d_counter + 1);
+            ctx->launches++;
+        }
+        c2a_solve_spec_kernel<<<blocks, kThreads, smem, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
+                                                             d_results, d_contacts, ctx->d_counter,
+                                                             user_order ? user_order : ctx->d_order, cap, nrec,
+                                                             ctx->d_spec);
+        ctx->launches++;
+        C2A_CUDA(cudaGetLastError());
+        return C2A_OK;
+    }
     if (prm.engine != C2A_ENGINE_THREAD) {
         /* the stack holds one pending pair per BVTT level: 2 depth + 2 entries */
         const int cap = 2 * deepest + 2 > 4 ? 2 * deepest + 2 : 4;
@@ -790,14 +640,6 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
         }
         const int most = ctx->sm_count * ctx->warp_blocks_per_sm;
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
-        if ((size_t)n > ctx->order_cap) {
-            C2A_CUDA(cudaStreamSynchronize(s));
-            if (ctx->d_order) cudaFree(ctx->d_order);
-            ctx->d_order = nullptr;
-            ctx->order_cap = 0;
-            C2A_CUDA(cudaMalloc(&ctx->d_order, sizeof(int32_t) * (size_t)n));
-            ctx->order_cap = (size_t)n;
-        }
         if (!user_order) { /* queries whose bounding spheres approach go first */
             C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 1, 0, 2 * sizeof(unsigned int), s));
             c2a_schedule_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_queries, n, ctx->d_models,
@@ -939,6 +781,7 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
         fprintf(stderr, "c2a_solve_batch_noalloc: only C2A_MODE_REFERENCE runs without allocations\n");
         return C2A_ERR_INVALID_ARGUMENT;
     }
+    std::lock_guard<std::mutex> lock(ctx->mu);
     const size_t num_models = ctx->models.size();
     if (num_models > C2A_NOALLOC_MAX_MODELS) {
         fprintf(stderr,
@@ -951,16 +794,25 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
     c2a_status st = check_depths(ctx);
     if (st) return st;
     unsigned char *scratch = nullptr;
-    st = noalloc_scratch(ctx->device, &scratch);
+    st = noalloc_scratch(ctx->device, &scratch); /* looked up by c2a_create; no CUDA call here */
     if (st) return st;
-    /* the model table on the stack, copied into the scratch array: no allocation on either side */
-    DevModel table[C2A_NOALLOC_MAX_MODELS];
-    for (size_t i = 0; i < num_models; i++) table[i] = dev_model_of(ctx->models[i]);
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     DevModel *d_table = reinterpret_cast<DevModel *>(scratch + kNoallocTableOffset);
     unsigned int *d_counter = reinterpret_cast<unsigned int *>(scratch);
-    if (num_models)
-        C2A_CUDA(cudaMemcpyAsync(d_table, table, sizeof(DevModel) * num_models, cudaMemcpyHostToDevice, s));
+    {
+        /* the model table is uploaded only when the array holds another
+         * context's table or this context's models changed since; the copy
+         * is from the stack, so wait for it before the frame goes away */
+        std::lock_guard<std::mutex> glock(g_noalloc_mu);
+        if (g_noalloc_table_gen[ctx->device] != ctx->models_gen) {
+            DevModel table[C2A_NOALLOC_MAX_MODELS];
+            for (size_t i = 0; i < num_models; i++) table[i] = dev_model_of(ctx->models[i]);
+            if (num_models)
+                C2A_CUDA(cudaMemcpyAsync(d_table, table, sizeof(DevModel) * num_models, cudaMemcpyHostToDevice, s));
+            C2A_CUDA(cudaStreamSynchronize(s));
+            g_noalloc_table_gen[ctx->device] = ctx->models_gen;
+        }
+    }
     C2A_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s)); /* the last call left its count here */
     c2a_params prm = *params;
     if (!d_contacts) prm.contacts_per_query = 0;
@@ -969,7 +821,6 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
                                                        d_contacts, d_counter);
     ctx->launches++;
     C2A_CUDA(cudaGetLastError());
-    /* the stack table is read by the copy engine before cudaMemcpyAsync returns (pageable source) */
     return C2A_OK;
 }
 

@@ -49,6 +49,16 @@ enum {
     ST_W_EXPAND, ST_W_EFAIL, ST_W_MKEXACT, ST_W_LEAF, ST_W_LEAF_X, ST_W_CYC_XFORM, ST_W_CYC_TEST_E,
     ST_W_CYC_TEST_X, ST_W_CYC_STORE, ST_W_CYC_DECIDE, ST_W_CYC_LEAF, ST_W_CYC_DFS, ST_W_CYC_QUERY,
     ST_W_CYC_X_RECT, ST_W_CYC_X_BOUND, ST_W_CYC_E_RECT, ST_W_CYC_E_BOUND,
+    /* the speculative engine: rounds, candidates, leaf candidates, lanes falling back to FP64,
+     * replay-side exact recomputes, exact distances, exact leaves, deferred-mint evaluations,
+     * pairs the replay decided; clock64 cycles per phase */
+    ST_S_ROUNDS, ST_S_CANDS, ST_S_LEAFC, ST_S_LANEX, ST_S_MKEXACT, ST_S_DISTX, ST_S_LEAFX, ST_S_FLUSHX,
+    ST_S_DECIDED, ST_S_CYC_REPLAY, ST_S_CYC_COLLECT, ST_S_CYC_EXPAND, ST_S_CYC_END,
+    /* speculation queue pops: stale, already decided or tested, pruned; rounds that stopped on an
+     * empty queue, on the pool */
+    ST_S_Q_STALE, ST_S_Q_SEEN, ST_S_Q_PRUNED, ST_S_STOP_EMPTY, ST_S_STOP_POOL,
+    /* per rotation step: the queue's and the pool's peak use, summed over steps, and the steps */
+    ST_S_QPEAK, ST_S_RECPEAK, ST_S_STEPS,
     ST_COUNT
 };
 constexpr int ST_W_FIRST = ST_W_EXPAND;

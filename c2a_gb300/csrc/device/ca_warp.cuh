@@ -37,6 +37,18 @@ namespace c2a {
 
 constexpr unsigned kWFull = 0xffffffffu;
 
+/* The warp-uniform state (the query, the speculative engine's bookkeeping)
+ * is written by every lane with the same value; the warp executes that code
+ * converged.  A host emulation of the warp, whose lanes do not run in
+ * lockstep, replaces these two: a per-lane query copy, and writes fenced by
+ * warp barriers so that no lane reads a location while another writes it. */
+#ifndef C2A_WARP_QUERY
+#define C2A_WARP_QUERY(sh) ((sh).q)
+#endif
+#ifndef C2A_WSET
+#define C2A_WSET(dst, v) ((dst) = (v))
+#endif
+
 /* 1: node-pair and leaf tests through the certified FP32 filter (FP64 only
  * where it cannot decide); 0: every test in FP64 */
 #ifndef C2A_WARP_FILTER
@@ -750,8 +762,16 @@ C2A_KDEV void toc_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, WarpShared &sh, 
     }
 }
 
-/* C2A_TimeOfContactStep, rotation branch (C2A.cpp:1855-1931) */
-C2A_KDEV void toc_step_warp(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, WarpShared &sh, int lane)
+/* the depth-first step traversal of the warp kernel */
+struct WarpDfs {
+    WarpShared &sh;
+    C2A_KDEV void operator()(Query &q, const M3 &R, V3 T, int lane) const { toc_dfs_warp(q, R, T, sh, lane); }
+};
+
+/* C2A_TimeOfContactStep, rotation branch (C2A.cpp:1855-1931); dfs runs
+ * TOCStepRecurse_Dis from the root pair */
+template <class Dfs>
+C2A_KDEV void toc_step_warp(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, const Dfs &dfs, int lane)
 {
     M3 R;
     V3 T;
@@ -773,7 +793,7 @@ C2A_KDEV void toc_step_warp(Query &q, M3 &R1, V3 &T1, M3 &R2, V3 &T2, WarpShared
     q.mint = 1;
     refresh_shadows(q);
     C2A_WCLOCK(d0);
-    toc_dfs_warp(q, R, T, sh, lane);
+    dfs(q, R, T, lane);
     C2A_WCLOCK(d1);
     C2A_WSTAT(q, ST_W_CYC_DFS, d1 - d0);
 }
@@ -894,10 +914,12 @@ C2A_KDEV int contact_dfs_warp(Query &q, const M3 &Rroot, V3 Troot, double thresh
 /* ------------------------------------------------------------ one query */
 
 /* C2A_Solve on one warp (reference order); lane 0 writes the result.  The
- * translation-only step runs the sequential code on every lane. */
+ * translation-only step runs the sequential code on every lane; dfs runs
+ * each rotation step's traversal. */
+template <class Dfs>
 C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int num_models, const c2a_params &prm,
                                c2a_result &out_g, c2a_contact *contacts, WarpShared &sh, Pending *tstack,
-                               int query_index, int lane)
+                               int query_index, int lane, const Dfs &dfs)
 {
     c2a_result out;
     memset(&out, 0, sizeof(out));
@@ -912,7 +934,7 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
         if (lane == 0) out_g = out;
         return;
     }
-    Query &q = sh.q; /* one copy per warp in shared memory, written with the same values by every lane */
+    Query &q = C2A_WARP_QUERY(sh); /* one copy per warp in shared memory, written with the same values by every lane */
 #ifdef C2A_STATS
     for (int i = 0; i < ST_COUNT; i++) q.st[i] = 0;
     for (int i = 0; i < ST_COUNT - ST_W_FIRST; i++) q.wst[i] = 0;
@@ -942,7 +964,7 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
     double toc = 0, lamda = 0.0, lastLamda = 0, dlamda = 0.0;
     bool collisionfree = false;
     if (translation) toc_step(q, R1, T1, R2, T2, true, tstack);
-    else toc_step_warp(q, R1, T1, R2, T2, sh, lane);
+    else toc_step_warp(q, R1, T1, R2, T2, dfs, lane);
     double dist = q.distance, mint = q.mint;
     if (translation) {
         collisionfree = (mint >= 1.0);
@@ -978,7 +1000,7 @@ C2A_KDEV void solve_query_warp(const c2a_query &in, const DevModel *models, int 
             motion_integrate(q.m2, lamda, R2.m, &T2.x, orn);
             set_pose1(q, R1, T1);
             q.upbound = 1.0 - lamda;
-            toc_step_warp(q, R1, T1, R2, T2, sh, lane);
+            toc_step_warp(q, R1, T1, R2, T2, dfs, lane);
             dist = q.distance;
             mint = q.mint;
         }

@@ -106,11 +106,17 @@ typedef struct c2a_params {
  * C2A_ENGINE_BATCHED  CANONICAL only: every query in lockstep CA iterations, each phase
  *                     a series of waves over all queries' node pairs (the call
  *                     synchronises the stream between waves);
- * C2A_ENGINE_THREAD   REFERENCE only: one thread per query. */
+ * C2A_ENGINE_THREAD   REFERENCE only: one thread per query;
+ * C2A_ENGINE_SPEC     REFERENCE only: one warp per query by speculative expansion
+ *                     and ordered replay -- each round the warp tests up to sixteen
+ *                     node pairs the reference's order is about to need (two lanes
+ *                     each, certified FP32 with FP64 where undecided), then replays
+ *                     the reference's decisions over them. */
 #define C2A_ENGINE_AUTO 0
 #define C2A_ENGINE_WARP 1
 #define C2A_ENGINE_BATCHED 2
 #define C2A_ENGINE_THREAD 3
+#define C2A_ENGINE_SPEC 4
 
 typedef struct c2a_result {
     int32_t collisionfree;
@@ -199,18 +205,23 @@ c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, 
  * memory at query time: code running under another allocator's fixed device
  * budget (an engine or simulator that hands out its own buffers and forbids
  * cudaMalloc after start-up), and real-time loops where cudaMalloc/cudaFree
- * would stall on their implicit device synchronisation.  It does what
- * c2a_solve_batch_device does (same kernel, same results, contacts in fixed
- * slots), but the kernel's scratch -- the work counter and the table of model
- * pointers -- lives in one file-scope device array of 8 KiB (room for
- * C2A_NOALLOC_MAX_MODELS models) that every GPU loading the library holds
- * until the process exits; no cudaMalloc, cudaFree or allocating library call
- * is made.  The models must have been built with c2a_model_build beforehand
- * (that call allocates).  The first call on a device looks up the array's
- * device address, so make that first call before any stream capture.  Calls
- * share the array: two calls whose kernels overlap on the GPU (different
- * streams) race; serialise them.  More than C2A_NOALLOC_MAX_MODELS models in
- * the context is rejected with C2A_ERR_NOALLOC_CAPACITY. */
+ * would stall on their implicit device synchronisation.  It gives the
+ * results of c2a_solve_batch_device (contacts in fixed slots) with the
+ * thread-per-query REFERENCE kernel, whatever params->engine says; its
+ * scratch -- the work counter and the table of model pointers -- lives in
+ * one file-scope device array of 8 KiB (room for C2A_NOALLOC_MAX_MODELS
+ * models) that every GPU loading the library holds until the process exits.
+ * No cudaMalloc, cudaFree or allocating library call is made.  The set-up
+ * (the array's device address and the kernel's module) is done by
+ * c2a_create, which allocates anyway.  The models must have been built with
+ * c2a_model_build beforehand (that call allocates); the first call after the
+ * context's model set changed copies the model table into the array and
+ * waits for that copy, later calls only clear the counter and launch.  Calls
+ * share the array and it keeps the last call's contents: two calls whose
+ * kernels overlap on the GPU (different streams, or contexts on the same
+ * device) race; serialise them.  More than C2A_NOALLOC_MAX_MODELS models in
+ * the context is rejected with C2A_ERR_NOALLOC_CAPACITY, CANONICAL mode with
+ * C2A_ERR_INVALID_ARGUMENT. */
 #define C2A_NOALLOC_MAX_MODELS 120
 c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
                                    const c2a_params *params, c2a_result *d_results, c2a_contact *d_contacts,
@@ -232,13 +243,13 @@ c2a_status c2a_toc_step_batch(c2a_context *ctx, const c2a_query *queries, int32_
 c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *threshold,
                                   int32_t contacts_per_query, c2a_result *results, c2a_contact *contacts);
 
-/* ---- motion (host) --------------------------------------------------- */
-/* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]
- * angular speed, out[4:7] linear velocity, out[7:11] begin quaternion
- * (x, y, z, w). */
+/* ---- ordered, hinted and distance batches ---------------------------- */
 /* c2a_solve_batch_device in C2A_MODE_REFERENCE (engine AUTO or WARP) taking
- * the queries in the caller's order: d_order (device int32) holds a
- * permutation of [0, n); entries outside [0, n) are skipped.  The order only
+ * the queries in the caller's order: d_order (device int32) must hold a
+ * permutation of [0, n).  Entries outside [0, n) are skipped; a duplicated
+ * index makes two warps write the same result and contact slots and leaves
+ * the left-out queries unwritten, so anything but a permutation gives
+ * undefined results.  The order only
  * decides which warp takes which query when (a schedule that starts the
  * costliest queries first shortens the batch); every result equals the
  * unordered call's.  The learned cost model of c2a_gb300/learned.py
@@ -276,6 +287,10 @@ c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, 
  * certified FP32 RSS bounds against the running minimum. */
 c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, c2a_distance_result *results);
 
+/* ---- motion (host) --------------------------------------------------- */
+/* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]
+ * angular speed, out[4:7] linear velocity, out[7:11] begin quaternion
+ * (x, y, z, w). */
 c2a_status c2a_motion_setup(const double *R0, const double *T0, const double *R1, const double *T1, double *out);
 /* Pose at time t (clamped to <= 1): R (9), T (3), qua (7: w, x, y, z, T). */
 c2a_status c2a_motion_integrate(const double *R0, const double *T0, const double *R1, const double *T1,

@@ -1,0 +1,79 @@
+"""The warp-per-query REFERENCE engines' device code on the CPU: 32 host
+threads emulate one warp (tests/cpp/warp_emu.h), so the speculative engine's
+replay, speculation and record bookkeeping -- and the sequential warp
+traversal it must agree with -- run here against the golden fixtures and the
+oracle port, bit for bit.  A warp collective reached by only some lanes
+aborts the emulation."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from c2a_testutil import describe, load_fixture, result_mismatches
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+WARP, SPEC = 1, 4
+SLOTS = 512
+
+
+@pytest.fixture(scope="module")
+def emu(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("emu") / "libspec_emu.so")
+    subprocess.run(["g++", "-std=c++20", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
+                    "-w", "-o", out, os.path.join(ROOT, "tests", "cpp", "spec_emu.cpp"),
+                    os.path.join(ROOT, "c2a_gb300", "csrc", "host", "bvh_build.cpp")], check=True)
+    lib = C.CDLL(out)
+    lib.spec_emu_model.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    lib.spec_emu_solve.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+    return lib
+
+
+def _run(lib, meshes_, qint, poses, params, engine):
+    from c2a_gb300 import api
+
+    lib.spec_emu_reset()
+    ids = []
+    for m in meshes_:
+        tv = np.ascontiguousarray(m.tri_verts())
+        vidx = np.ascontiguousarray(m.faces, dtype=np.int32)
+        ids.append(lib.spec_emu_model(m.num_tris, tv.ctypes.data, vidx.ctypes.data))
+    q = qint.copy()
+    q[:, 0] = np.asarray(ids)[qint[:, 0]]
+    q[:, 1] = np.asarray(ids)[qint[:, 1]]
+    qs = api.make_queries(q, poses)
+    prm = api.make_params(dict(params, engine=engine), SLOTS)
+    n = len(q)
+    res = np.zeros(n, dtype=api.RESULT_DTYPE)
+    con = np.zeros(n * SLOTS, dtype=api.CONTACT_DTYPE)
+    lib.spec_emu_solve(qs.ctypes.data, n, C.byref(prm), res.ctypes.data, con.ctypes.data, 120.0)
+    return res, con.reshape(n, SLOTS)
+
+
+@pytest.mark.parametrize("engine", [WARP, SPEC])
+@pytest.mark.parametrize("name", ["config1", "mixed", "translation"])
+def test_emulated_engine_matches_fixture(emu, name, engine):
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    sel = np.linspace(0, len(qint) - 1, 6).astype(int)
+    res, con = _run(emu, ms, qint[sel], poses[sel], params, engine)
+    flat = np.concatenate([econ[off[i]:off[i + 1]][:SLOTS] for i in sel])
+    offs = np.concatenate([[0], np.cumsum([min(SLOTS, off[i + 1] - off[i]) for i in sel])])
+    bad = result_mismatches(res, exp[sel], con, flat, offs)
+    assert not bad, f"engine {engine}: " + describe(res, exp[sel], bad[0])
+
+
+def test_emulated_spec_matches_port_small_models(emu, port):
+    """Small knots (many leaves per round), an iteration cap, and tiny models."""
+    from c2a_gb300 import workloads
+
+    for wl, prm in ((workloads.small_knots(10, seed=41, device="cpu"), None),
+                    (workloads.small_knots(6, seed=42, device="cpu"), {"max_iters": 2}),
+                    (workloads.small_knots(6, seed=43, segments=4, around=3, device="cpu"), None)):
+        params = dict(wl.params, **(prm or {}))
+        res, con = _run(emu, wl.meshes, wl.qint, wl.poses, params, SPEC)
+        pres, pcon = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, params, contacts_per_query=SLOTS)
+        flat = np.concatenate([pcon[q][:min(SLOTS, pres[q]["num_contact"])] for q in range(wl.n)])
+        offs = np.concatenate([[0], np.cumsum(np.minimum(SLOTS, pres["num_contact"]))])
+        bad = result_mismatches(res, pres, con, flat, offs)
+        assert not bad, describe(res, pres, bad[0])
