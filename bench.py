@@ -43,6 +43,7 @@ UNIT = "queries/s"
 NODE_BYTES = 208   # FP64 node fields a BV test reads (R, Tr, l, r, angularRadius, R_loc, first_child)
 TRI_BYTES = 144    # two triangles (9 doubles each) per triangle test
 CONTACT_SLOTS = 64
+REFERENCE_SAMPLE = 16384  # queries per step of the CPU arms (evenly strided over the batch)
 
 
 def parse():
@@ -131,66 +132,52 @@ def measured_peaks() -> dict:
         return {}
 
 
-def profile_traffic():
-    """DRAM bytes per query of the CA kernel from the committed ncu summary (or None)."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "ca_kernel_config2.json")) as fh:
-            return json.load(fh)
-    except (OSError, ValueError):
-        return None
+def strided(n: int, sample: int) -> np.ndarray:
+    """``sample`` query indices spread evenly over a batch of ``n``."""
+    sample = max(1, min(sample, n))
+    return np.unique(np.linspace(0, n - 1, sample).astype(np.int64))
 
 
-def cpu_baseline(wl, sample: int, threads: int):
-    """The oracle port (the reference's algorithm, bit-identical) on host threads."""
+def cpu_baseline(wl, idx, threads: int):
+    """The oracle port (the reference's algorithm, bit-identical) on host threads,
+    over the queries ``idx`` of ``wl``."""
     from oracle.oracle import Port, build
 
     build(ref=False)
     port = Port()
     models = port.models(wl.meshes)
-    sub = wl.subset(np.arange(min(sample, wl.n)))
+    sub = wl.subset(idx)
     t0 = time.perf_counter()
-    res, _ = port.solve_batch(models, sub.qint, sub.poses, sub.params, threads=threads,
-                              contacts_per_query=CONTACT_SLOTS)
+    res, con = port.solve_batch(models, sub.qint, sub.poses, sub.params, threads=threads,
+                                contacts_per_query=CONTACT_SLOTS)
     dt = time.perf_counter() - t0
-    return sub.n / dt, dt, res
-
-
-def auto_sample(wl, threads: int, target_s: float = 12.0) -> int:
-    from oracle.oracle import Port, build
-
-    build(ref=False)
-    port = Port()
-    models = port.models(wl.meshes)
-    sub = wl.subset(np.arange(min(64, wl.n)))
-    t0 = time.perf_counter()
-    port.solve_batch(models, sub.qint, sub.poses, sub.params, threads=threads, contacts_per_query=CONTACT_SLOTS)
-    per_query_wall = (time.perf_counter() - t0) / sub.n
-    return int(np.clip(target_s / max(per_query_wall, 1e-9), 256, wl.n))
+    return sub.n / dt, dt, res, con
 
 
 def run_reference(args, rank, world):
-    """--impl reference: CPU oracle port of the reference on all host cores."""
+    """--impl reference: the CPU oracle port of the reference on all host
+    cores, over an evenly strided sample of the same batch (placed on the host)."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    wl = workloads.config2(n=args.queries, seed=2, device="cpu", subset=args.cpu_sample or 4096)
-    sample = args.cpu_sample or auto_sample(wl, threads, target_s=10.0)
-    sample = min(sample, wl.n)
+    idx = strided(args.queries, args.cpu_sample or REFERENCE_SAMPLE)
+    wl = workloads.config2(n=args.queries, seed=2, device="cpu", indices=idx)
+    all_idx = np.arange(wl.n)
     rates, times = [], []
     for _ in range(args.warmup):
-        cpu_baseline(wl, min(sample, 256), threads)
+        cpu_baseline(wl, all_idx[:min(256, wl.n)], threads)
     for _ in range(args.steps):
-        r, dt, _ = cpu_baseline(wl, sample, threads)
+        r, dt, _, _ = cpu_baseline(wl, all_idx, threads)
         rates.append(r)
         times.append(dt)
-    value = float(sample * len(times) / sum(times))
+    value = float(wl.n * len(times) / sum(times))
+    sample = f"{wl.n} of the {args.queries} queries, evenly strided, every step"
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
             "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
-            "config": config_dict(wl, args, sample_only=sample),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"first {sample} of the {wl.n} config-2 queries per step"},
+            "config": config_dict(wl, args, queries=args.queries), "implementation": implementation_dict(args),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -202,21 +189,33 @@ KERNELS = {("reference", "auto"): "c2a_solve_warp_kernel", ("reference", "warp")
            ("canonical", "warp"): "c2a_canonical_kernel", ("canonical", "batched"): "k_dsearch"}
 
 
-def config_dict(wl, args, sample_only=None):
-    traversal = ("reference order (FP64, bit-identical to the reference); one warp per query, each node-pair "
-                 "test split across the lanes" if args.mode == "reference" else
-                 "canonical: each step seeded with the exact closest pair (the reference's C2A_Distance), "
-                 "order-free front traversal; bit-identical to that composition of the reference's functions")
-    return {"workload": wl.name, "queries": wl.n if sample_only is None else int(sample_only),
+def config_dict(wl, args, queries=None):
+    """The workload (identical for both arms); how it runs is in implementation_dict."""
+    return {"workload": wl.name, "queries": wl.n if queries is None else int(queries),
             "triangles_per_model": wl.meshes[0].num_tris, "models": "two (2,3) torus-knot tubes, 400 x 50",
             "th_ca": wl.params["th_ca"], "t_delta": wl.params["tol_t"], "qsize": wl.params["qsize"],
-            "mode": args.mode, "engine": args.engine, "traversal": traversal,
+            "mode": args.mode,
             "seeding": "plain (triangle 0 of each model, as after EndModel); the learned seeding is measured "
                        "by --mode learned (CANONICAL mode only: REFERENCE results depend on the seed)",
-            "order": ("not applicable: the CPU port, queries split statically over the threads"
-                      if args.impl == "reference" else args.order if args.mode == "reference" else "geometric"),
-            "contacts_per_query": CONTACT_SLOTS, "l2": "flushed between timed steps (256 MiB write)",
-            "parallelism": f"replicas x{args.gpus}"}
+            "contacts_per_query": CONTACT_SLOTS, "parallelism": f"replicas x{args.gpus}"}
+
+
+def implementation_dict(args):
+    if args.impl == "reference":
+        return {"what": "the CPU oracle port of the reference (bit-identical to the reference compiled here), "
+                        "one query per task, all host threads"}
+    traversal = {"spec": "reference order by speculative expansion and ordered replay: each warp round tests up to "
+                         "16 node pairs the order is about to need (two lanes each, certified FP32 with FP64 where "
+                         "undecided), then replays the reference's decisions (FP64, bit-identical)",
+                 "warp": "reference order (FP64, bit-identical to the reference); one warp per query, each "
+                         "node-pair test split across the lanes",
+                 "thread": "reference order, one thread per query"}
+    return {"engine": args.engine, "order": args.order if args.mode == "reference" else "geometric",
+            "traversal": traversal.get(ENGINE_OF.get(args.engine, args.engine), "canonical front")
+            if args.mode == "reference" else
+            "canonical: each step seeded with the exact closest pair (the reference's C2A_Distance), order-free "
+            "front traversal; bit-identical to that composition of the reference's functions",
+            "l2": "flushed between timed steps (256 MiB write)"}
 
 
 def run_learned(args, rank, world, local):
@@ -459,20 +458,28 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        sample = args.cpu_sample or auto_sample(wl, threads)
-        rate, dt, pres = cpu_baseline(wl, sample, threads)
-        same = bool((pres["toc"].tobytes() == res["toc"][:len(pres)].tobytes()) and
-                    np.array_equal(pres["numCA"], res["numCA"][:len(pres)]))
+        idx = strided(n, args.cpu_sample or REFERENCE_SAMPLE)
+        rate, dt, pres, pcon = cpu_baseline(wl, idx, threads)
+        cont = d_c.cpu().numpy().view(api.CONTACT_DTYPE).reshape(n, CONTACT_SLOTS)
+        fields = ("collisionfree", "numCA", "translation", "num_contact", "toc", "distance", "mint", "num_bv_tests",
+                  "num_tri_tests", "seed_a", "seed_b", "R_toc", "T_toc")
+        same = all(pres[f].tobytes() == res[f][idx].tobytes() for f in fields)
+        for k, i in enumerate(idx):
+            m = min(int(pres[k]["num_contact"]), CONTACT_SLOTS)
+            for f in ("type_a", "type_b", "fid_a", "fid_b", "tri_a", "tri_b", "pa", "pb", "distance"):
+                same = same and cont[i][:m][f].tobytes() == pcon[k][:m][f].tobytes()
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"first {len(pres)} of the {n} queries ({dt:.1f} s wall on {threads} threads)",
-               "bit_identical_to_gpu": same}
+               "sample": f"{len(idx)} of the {n} queries, evenly strided ({dt:.1f} s wall on {threads} threads)",
+               "bit_identical_to_gpu": bool(same),
+               "compared": "every result field (flags, TOC, iterations, distance, mint, counters, seeds, TOC poses) "
+                           "and every contact in its slots"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
-                "config": config_dict(wl, args), "clocks": clk, "gpu_launches": launches, "e2e": e2e,
+                "config": config_dict(wl, args), "implementation": implementation_dict(args), "clocks": clk, "gpu_launches": launches, "e2e": e2e,
                 "roofline": roofline, "cpu_baseline": cpu,
                 "learned_order": learned_info,
                 "collision_fraction": float(1 - res["collisionfree"].mean()),

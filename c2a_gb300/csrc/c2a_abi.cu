@@ -23,6 +23,11 @@
 
 using namespace c2a;
 
+/* records of the speculative engine beyond the replay's path */
+#ifndef C2A_SPEC_EXTRA
+#define C2A_SPEC_EXTRA 64
+#endif
+
 namespace {
 
 constexpr int kThreads = kBlockThreads;
@@ -578,7 +583,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
         /* the stack holds one pending pair per BVTT level: 2 depth + 2 entries;
          * records: the replay's path (one per BVTT level) plus 64 for speculation */
         const int cap = 2 * deepest + 2 > 4 ? 2 * deepest + 2 : 4;
-        const int nrec = 2 * deepest + 2 + 64;
+        const int nrec = 2 * deepest + 2 + C2A_SPEC_EXTRA;
         const size_t per = warp_shared_bytes(cap) + spec_shared_bytes(nrec);
         const size_t smem = per * (kThreads / 32);
         if (!ctx->spec_smem_attr) {

@@ -59,6 +59,8 @@ enum {
     ST_S_Q_STALE, ST_S_Q_SEEN, ST_S_Q_PRUNED, ST_S_STOP_EMPTY, ST_S_STOP_POOL,
     /* per rotation step: the queue's and the pool's peak use, summed over steps, and the steps */
     ST_S_QPEAK, ST_S_RECPEAK, ST_S_STEPS,
+    /* inside the test phase: the lane tests, the leaf tasks */
+    ST_S_CYC_TEST, ST_S_CYC_LEAF,
     ST_COUNT
 };
 constexpr int ST_W_FIRST = ST_W_EXPAND;

@@ -58,8 +58,9 @@ enum : uint16_t {
     SF_DONE = 4,   /* leaf: tri and lm hold its certified distance and mint */
     SF_LBAD = 8,   /* leaf: the filter could not certify the triangle distance */
     SF_MBAD = 16,  /* leaf: ... nor its mint */
-    SF_USED = 32,  /* the replay has decided this pair */
-    SF_FLIGHT = 64 /* a candidate of the current round */
+    SF_USED = 32,   /* the replay has decided this pair */
+    SF_FLIGHT = 64, /* a candidate of the current round */
+    SF_LEXACT = 128 /* leaf: the exact triangle distance and leaf mint are in the record's global part */
 };
 
 /* a child pair of a record (shared memory, 48 bytes) */
@@ -84,6 +85,7 @@ struct SpecRec {
 struct SpecRecG {
     double R[9], T[3];   /* the expanded pair's exact transform */
     double dx[2], mx[2]; /* the children's exact d and mint (SF_EXACT) */
+    double tx[2], tm[2]; /* leaf children: exact triangle distance and leaf mint (SF_LEXACT) */
 };
 
 /* a contribution to the step's mint that may be the minimum (global scratch) */
@@ -410,6 +412,21 @@ C2A_KDEV void spec_leaf(Query &q, SpecCtx &c, uint32_t ref, int lane)
     const SpecEnt &e = spec_ent(c, ref);
     const int b1 = e.b1, b2 = e.b2;
     const uint16_t fl = e.flags;
+    if (fl & SF_LEXACT) { /* the lane computed it in FP64: the reference's comparison directly */
+        const double dTri = c.g[ref >> 1].tx[ref & 1], mint = c.g[ref >> 1].tm[ref & 1];
+        spec_exact_distance(q, c, lane);
+        if (dTri <= q.distance) {
+            q.distance = dTri;
+            c.dist_x = dTri;
+            c.dist_exact = true;
+            c.dist_b1 = b1;
+            c.dist_b2 = b2;
+            if (mint <= c.mint_x) c.mint_x = mint;
+            refresh_shadows(q);
+            c.dist_e = q.distance_e;
+        }
+        return;
+    }
     const EF tri = e.tri, lm = e.lm;
     const int le = (fl & SF_LBAD) ? -1 : ef_le3(tri, c.dist_e);
     if (le == 0) return;
@@ -620,11 +637,26 @@ C2A_KDEV int spec_collect(Query &q, SpecCtx &c, uint32_t due)
 
 /* ----------------------------------------------------------------- test */
 
-/* the leaf task of one lane: certified triangle distance and leaf mint */
-C2A_KDEV void spec_leaf_task(const Query &q, SpecEnt &e)
+/* the leaf task of one lane: certified triangle distance and leaf mint
+ * (C2A_SPEC_FP64: the exact ones) */
+C2A_KDEV void spec_leaf_task(const Query &q, SpecCtx &sc, uint32_t ref)
 {
+    SpecEnt &e = spec_ent(sc, ref);
     const int b1 = e.b1, b2 = e.b2;
     const int ia = -__ldg(&q.A->nodes[b1].first_child) - 1, ib = -__ldg(&q.B->nodes[b2].first_child) - 1;
+#ifdef C2A_SPEC_FP64
+    {
+        V3 p, qq;
+        TriFeat f;
+        bool col = false;
+        const double dTri = tri_distance_x(q, ia, ib, p, qq, f, col);
+        const int r = (int)(ref >> 1), s = (int)(ref & 1);
+        sc.g[r].tx[s] = dTri;
+        sc.g[r].tm[s] = spec_leaf_mint_x(q, b1, b2, dTri, p, qq);
+        e.flags = (uint16_t)((e.flags & ~SF_FLIGHT) | SF_DONE | SF_LEXACT);
+        return;
+    }
+#endif
     EFCtx c{!q.shadows_ok};
     V3T<EF> S[3], T[3], t[3];
     load_tri_e(S, q.A->stris + ia);
@@ -656,6 +688,48 @@ C2A_KDEV void spec_leaf_task(const Query &q, SpecEnt &e)
     e.tri = dTri;
     e.lm = lm;
     e.flags = (uint16_t)((e.flags & ~SF_FLIGHT) | fl);
+}
+
+/* C2A_BV_Distance and both motion bounds of child pair (x1, x2) of a pair
+ * placed by (PRe, PTe) (C2A.cpp:1195-1274), through the certified FP32
+ * filter on one lane: the child transform, RectDist with the cases through
+ * one code path (rect_dist_lane), d = max(z, 0) and mint.  Returns false
+ * when a decision cannot be certified (the caller recomputes in FP64). */
+C2A_KDEV bool spec_bv_test_e(const Query &q, int side, const M3T<EF> &PRe, V3T<EF> PTe, int x1, int x2, EF &d,
+                             EF &mint, bool &d_zero)
+{
+    EFCtx c{false};
+    NodeE n1, n2;
+    load_e(n1, q.A->snodes + x1);
+    load_e(n2, q.B->snodes + x2);
+    M3T<EF> R;
+    V3T<EF> T;
+    if (side == 0) {
+        R = tmmul(n1.R, PRe);
+        T = tmul(n1.R, PTe - n1.Tr);
+    } else {
+        R = mmul(PRe, n2.R);
+        T = mul_add(PRe, n2.Tr, PTe);
+    }
+    V3T<EF> S = v3t(ef_exact(0), ef_exact(0), ef_exact(0));
+    const EF z = rect_dist_lane(R, T, n1.l, n2.l, S, c) - (n1.r + n2.r);
+    if (c.bad) return false;
+    const int pos = ef_lt3(ef_exact(0), z);
+    if (pos < 0) return false;
+    if (pos == 0) {
+        d_zero = true;
+        d = ef_exact(0);
+        mint = ef_exact(0);
+        return true;
+    }
+    d_zero = false;
+    d = z;
+    V3T<EF> S1 = mul(q.r1e, mul(n1.Rloc, S));
+    V3T<EF> S2 = mul_s(S1, ef_exact(-1));
+    const EF mb1 = bound_rss(q.e1, n1.angR, S1, c);
+    const EF mb2 = bound_rss(q.e2, n2.angR, S2, c);
+    mint = max0_c(ef_div(d, mb1 + mb2, c));
+    return !c.bad;
 }
 
 /* one output of a child transform (the expression trees of tmmul/tmul for
@@ -762,7 +836,17 @@ C2A_KDEV void spec_expand(const Query &q, SpecCtx &c, int ncand, const M3 &Rroot
     const V3T<EF> Te = ef_v3(T, ec);
     EF d = ef_exact(0.0f), m = ef_exact(0.0f);
     bool dz = false;
-    const bool ok = !ec.bad && bv_test_e(q, side, Re, Te, x1, x2, d, m, dz);
+#ifdef C2A_STATS
+    __syncwarp();
+    C2A_WCLOCK(x1c);
+#endif
+#ifdef C2A_SPEC_FP64
+    const bool ok = false; /* every lane test in FP64 */
+    (void)Re;
+    (void)Te;
+#else
+    const bool ok = !ec.bad && spec_bv_test_e(q, side, Re, Te, x1, x2, d, m, dz);
+#endif
 #ifdef C2A_STATS
     {
         const int nx = __popc(__ballot_sync(kWFull, do_exp && !ok));
@@ -786,6 +870,11 @@ C2A_KDEV void spec_expand(const Query &q, SpecCtx &c, int ncand, const M3 &Rroot
         m = in_d(mx, cc);
         if (cc.bad) d = m = EF{0.0f, __int_as_float(0x7f800000)};
     }
+#ifdef C2A_STATS
+    __syncwarp();
+    C2A_WCLOCK(x2c);
+    C2A_WSTAT(q, ST_S_CYC_TEST, x2c - x1c);
+#endif
     /* d2 < d1: child c (lane sub 1) first? (C2A.cpp:1281) */
     const EF dp = EF{__shfl_xor_sync(kWFull, d.v, 1), __shfl_xor_sync(kWFull, d.e, 1)};
     const EF da = sub ? dp : d, dc = sub ? d : dp;
@@ -833,7 +922,16 @@ C2A_KDEV void spec_expand(const Query &q, SpecCtx &c, int ncand, const M3 &Rroot
         }
     }
     /* leaf candidates: the triangle distance on the slot's first lane */
-    if (is_leaf && sub == 0) spec_leaf_task(q, spec_ent(c, ref));
+#ifdef C2A_STATS
+    __syncwarp();
+    C2A_WCLOCK(x3c);
+#endif
+    if (is_leaf && sub == 0) spec_leaf_task(q, c, ref);
+#ifdef C2A_STATS
+    __syncwarp();
+    C2A_WCLOCK(x4c);
+    C2A_WSTAT(q, ST_S_CYC_LEAF, x4c - x3c);
+#endif
 }
 
 /* ------------------------------------------------------------- the step */

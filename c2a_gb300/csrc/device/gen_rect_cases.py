@@ -232,6 +232,89 @@ def main():
         w(line)
     w("}")
     w("")
+    lane_lines = []
+    lw = lane_lines.append
+    # the whole distance on one lane: preamble once, the cases in order with
+    # their operands picked per case, the winner's value once
+    lw("/* C2ARectDist on one lane without diverging across the cases: the preamble")
+    lw(" * once, then the sixteen cases in the reference's order, each through the")
+    lw(" * same code path with its operands picked by a switch, until one holds; its")
+    lw(" * edge-pair distance, or the face-separation tail when none does.  Same")
+    lw(" * expression trees and the same first-hit rule as rect_dist; with the FP32")
+    lw(" * filter an undecided case sets ctx.bad (the caller recomputes in FP64). */")
+    lw("template <class T, class C>")
+    lw("C2A_DEV T rect_dist_lane(const M3T<T> &Rab, V3T<T> Tab, const T a[2], const T b[2], V3T<T> &S, C &ctx)")
+    lw("{")
+    for line in pre.strip("\n").split("\n"):
+        lw(line)
+    for e, name in exprs.items():
+        lw(f"    const T {name} = {e};")
+    lw("    int win = -1;")
+    lw("#pragma unroll 1")
+    lw("    for (int j = 0; j < 16 && !ctx.bad; j++) {")
+    lw("        T L[4], R[4], s1[7], s2[7];")
+    lw("        switch (j) {")
+    for j, r in enumerate(rows):
+        lw(f"        case {j}:")
+        for i, (l_, r_) in enumerate(r["c"]):
+            lw(f"            L[{i}] = {l_}; R[{i}] = {r_};")
+        lw("            " + " ".join(f"s1[{i}] = {v};" for i, v in enumerate(r["s1"])))
+        lw("            " + " ".join(f"s2[{i}] = {v};" for i, v in enumerate(r["s2"])))
+        lw("            break;")
+    lw("        default:")
+    lw("            break;")
+    lw("        }")
+    lw("        C c0 = ctx, c1 = ctx, c2 = ctx, c3 = ctx, ci1 = ctx, ci2 = ctx;")
+    lw("        const bool k0 = cmp_lt(L[0], R[0], c0, 0), k1 = cmp_lt(L[1], R[1], c1, 0);")
+    lw("        const int t0 = c0.bad ? -1 : k0, t1 = c1.bad ? -1 : k1;")
+    lw("        if (rc_and3(t0, t1) == 0) continue; /* the usual outcome: no in_slab needed */")
+    lw("        const bool k2 = cmp_lt(L[2], R[2], c2, 0), k3 = cmp_lt(L[3], R[3], c3, 0);")
+    lw("        const int t2 = c2.bad ? -1 : k2, t3 = c3.bad ? -1 : k3;")
+    lw("        int u1 = 1, u2 = 1;")
+    lw("        if (t2 != 1) {")
+    lw("            const bool i1 = in_slab(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], s1[6], ci1);")
+    lw("            u1 = ci1.bad ? -1 : i1;")
+    lw("        }")
+    lw("        if (t3 != 1) {")
+    lw("            const bool i2 = in_slab(s2[0], s2[1], s2[2], s2[3], s2[4], s2[5], s2[6], ci2);")
+    lw("            u2 = ci2.bad ? -1 : i2;")
+    lw("        }")
+    lw("        const int hit = rc_and3(rc_and3(t0, t1), rc_and3(rc_or3(t2, u1), rc_or3(t3, u2)));")
+    lw("        if (hit < 0) ctx.bad = true;")
+    lw("        else if (hit == 1) {")
+    lw("            win = j;")
+    lw("            break;")
+    lw("        }")
+    lw("    }")
+    lw("    if (ctx.bad) return zero;")
+    lw("    if (win < 0) return rect_tail(Rab, Tab, a, b, S, ctx);")
+    lw("    T e[5], qb = zero;")
+    lw("    int px = 0, py = 0, qkind = 1, cb = 0, cu = 0;")
+    lw("    switch (win) {")
+    for j, r in enumerate(rows):
+        lw(f"    case {j}:")
+        lw("        " + " ".join(f"e[{i}] = {v};" for i, v in enumerate(r["e"])))
+        lw(f"        px = {pt(r['px'])}; py = {pt(r['py'])}; qkind = {r['qkind']}; cb = {r['cb']}; qb = {r['qb']};"
+          f" cu = {r['cu']};")
+        lw("        break;")
+    lw("    default:")
+    lw("        break;")
+    lw("    }")
+    lw("    T t, u;")
+    lw("    edge_params(t, u, e[0], e[1], e[2], e[3], e[4], ctx);")
+    lw("    const T Px = px == 0 ? a[0] : px == 1 ? a[1] : px == 4 ? t : zero;")
+    lw("    const T Py = py == 0 ? a[0] : py == 1 ? a[1] : py == 4 ? t : zero;")
+    lw("    const V3T<T> P = v3t<T>(Px, Py, zero);")
+    lw("    const T rbx = cb ? Rab.m[1] : Rab.m[0], rby = cb ? Rab.m[4] : Rab.m[3], rbz = cb ? Rab.m[7] : Rab.m[6];")
+    lw("    const T rux = cu ? Rab.m[1] : Rab.m[0], ruy = cu ? Rab.m[4] : Rab.m[3], ruz = cu ? Rab.m[7] : Rab.m[6];")
+    lw("    const V3T<T> Q2 = v3t(Tab.x + rbx * qb + rux * u, Tab.y + rby * qb + ruy * u, Tab.z + rbz * qb + ruz * u);")
+    lw("    const V3T<T> Q1 = v3t(Tab.x + rux * u, Tab.y + ruy * u, Tab.z + ruz * u);")
+    lw("    const V3T<T> Q = qkind == 2 ? Q2 : Q1;")
+    lw("    S = v3t(Q.x - P.x, Q.y - P.y, Q.z - P.z);")
+    lw("    return num_sqrt(dot(S, S));")
+    lw("}")
+    lw("")
+    lines.extend(lane_lines)
     w("} // namespace c2a")
     w("#endif")
     open(OUT, "w").write("\n".join(lines) + "\n")

@@ -155,10 +155,12 @@ def place_at_gap(mesh_a: Mesh, mesh_b: Mesh, R0: np.ndarray, u: np.ndarray, gap:
 
 def ccd_queries(mesh_a: Mesh, mesh_b: Mesh, n: int, seed: int, gap_range=(0.05, 1.0), speed_range=(0.5, 3.0),
                 speed_log=False, cone_deg: float = 30.0, max_rot: float = np.pi, device: str | None = None,
-                model_a: int = 0, model_b: int = 1, subset: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+                model_a: int = 0, model_b: int = 1, subset: int | None = None,
+                indices: np.ndarray | None = None) -> tuple[np.ndarray, np.ndarray]:
     """``n`` queries of the benchmark family: returns (qint (n, 4), poses (n, 48)).
     With ``subset`` only the first ``subset`` of the n queries are placed and
-    returned (same random draws as the full set)."""
+    returned, with ``indices`` only those queries (same random draws as the
+    full set either way)."""
     rng = np.random.default_rng(seed)
     diag = mesh_a.bbox_diag()
     R0b = random_rotations(rng, n)
@@ -174,6 +176,10 @@ def ccd_queries(mesh_a: Mesh, mesh_b: Mesh, n: int, seed: int, gap_range=(0.05, 
     if subset is not None and subset < n:
         n = subset
         R0b, u, gap, speed, vdir, axis, ang = (x[:n] for x in (R0b, u, gap, speed, vdir, axis, ang))
+    if indices is not None:
+        idx = np.asarray(indices)
+        n = len(idx)
+        R0b, u, gap, speed, vdir, axis, ang = (x[idx] for x in (R0b, u, gap, speed, vdir, axis, ang))
     T0b = place_at_gap(mesh_a, mesh_b, R0b, u, gap, device=device)
     T1b = T0b + speed[:, None] * vdir
     R1b = np.einsum("nij,njk->nik", R0b, axis_angle(axis, ang))
@@ -210,12 +216,14 @@ def config1(n: int = 1000, seed: int = 1, device: str | None = None) -> Workload
     return Workload("config1_torusknot3200_1000q", [knot], qint, poses, default_params(knot.bbox_diag(), 1e-3, 40))
 
 
-def config2(n: int = 65536, seed: int = 2, device: str | None = None, subset: int | None = None) -> Workload:
+def config2(n: int = 65536, seed: int = 2, device: str | None = None, subset: int | None = None,
+            indices: np.ndarray | None = None) -> Workload:
     """Same family at 400 x 50 = 40,000 triangles, 65,536 queries,
-    th_ca = 1e-4 diag, qsize 64, about 30% colliding within t in [0, 1]."""
+    th_ca = 1e-4 diag, qsize 64, about 30% colliding within t in [0, 1].
+    ``subset``/``indices`` place only some of the n queries (see ccd_queries)."""
     knot = torus_knot(2, 3, 400, 50, 1.0, 0.15)
     qint, poses = ccd_queries(knot, knot, n, seed, device=device, model_a=0, model_b=0, subset=subset,
-                              cone_deg=CONFIG2_CONE_DEG)
+                              cone_deg=CONFIG2_CONE_DEG, indices=indices)
     return Workload("config2_torusknot40000_65536q", [knot], qint, poses, default_params(knot.bbox_diag(), 1e-4, 64))
 
 

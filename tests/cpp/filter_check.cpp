@@ -156,6 +156,22 @@ int c2a_fc_bv(const double *PR, const double *PT, const double *f1, const double
     out[6] = c.bad ? 0.0 : 1.0;
     out[7] = c.where;
     out[8] = zero;
+    /* the one-lane form of the speculative engine (rect_dist_lane): d.v, d.e, certified, zero flag */
+    EFCtx cl{false};
+    V3T<EF> Sl = v3t(ef_exact(0), ef_exact(0), ef_exact(0));
+    const EF zl = rect_dist_lane(Re, Te, ea.l, eb.l, Sl, cl) - (ea.r + eb.r);
+    EF dl = ef_exact(0);
+    int zl0 = 0;
+    if (!cl.bad) {
+        const int pos = ef_lt3(ef_exact(0), zl);
+        if (pos < 0) C2A_EF_FAIL(cl, 100001);
+        else if (pos == 0) zl0 = 1;
+        else dl = zl;
+    }
+    out[9] = dl.v;
+    out[10] = dl.e;
+    out[11] = cl.bad ? 0.0 : 1.0;
+    out[12] = zl0;
     return 0;
 }
 
@@ -237,6 +253,24 @@ int c2a_fc_rect_lanes(const double *Rab9, const double *Tab3, const double *a, c
     out[4] = d;
     out[5] = Sw.x; out[6] = Sw.y; out[7] = Sw.z;
     out[8] = win;
+    return 0;
+}
+
+/*
+ * C2ARectDist on one lane (rect_dist_lane: the cases through one code path in
+ * order) next to the sequential rect_dist, FP64.  out: d_seq, S_seq[3], d_lane,
+ * S_lane[3].
+ */
+int c2a_fc_rect_one_lane(const double *Rab9, const double *Tab3, const double *a, const double *b, double *out)
+{
+    const M3 R = m3_of(Rab9);
+    const V3 T = v3(Tab3[0], Tab3[1], Tab3[2]);
+    ExactCtx xc{false};
+    V3 S = v3(0, 0, 0), Sl = v3(0, 0, 0);
+    out[0] = rect_dist(R, T, a, b, S, xc);
+    out[1] = S.x; out[2] = S.y; out[3] = S.z;
+    out[4] = rect_dist_lane(R, T, a, b, Sl, xc);
+    out[5] = Sl.x; out[6] = Sl.y; out[7] = Sl.z;
     return 0;
 }
 

@@ -42,8 +42,8 @@ def _walk(fc, mesh, poses, walks, rng):
     ctx = api.Context(-1)
     mid = ctx.model(mesh)
     f, fch, tv, _, _ = ctx.download(mid)
-    out = np.zeros(9)
-    rec = {"bv": 0, "bv_ok": 0, "tri": 0, "tri_ok": 0, "viol": []}
+    out = np.zeros(16)
+    rec = {"bv": 0, "bv_ok": 0, "bv_lane_ok": 0, "tri": 0, "tri_ok": 0, "viol": []}
     for P in poses:
         R1, T1 = P[0:9].reshape(3, 3), P[9:12]
         R2, T2 = P[24:33].reshape(3, 3), P[33:36]
@@ -77,6 +77,13 @@ def _walk(fc, mesh, poses, walks, rng):
                         elif abs(out[2] - out[0]) > out[3] or (
                                 np.isfinite(out[1]) and abs(out[4] - out[1]) > out[5]):
                             rec["viol"].append(("bv", out.copy()))
+                    if out[11] == 1:  # the one-lane RectDist of the speculative engine
+                        rec["bv_lane_ok"] += 1
+                        if out[12] == 1:
+                            if out[0] != 0.0:
+                                rec["viol"].append(("lane zero", out.copy()))
+                        elif abs(out[9] - out[0]) > out[10]:
+                            rec["viol"].append(("lane", out.copy()))
                     kids.append((out[0], ci, cj))
                 k = 0 if kids[0][0] <= kids[1][0] else 1
                 if rng.random() < 0.3:
@@ -98,6 +105,7 @@ def test_filter_bounds_hold_config2(fc):
     assert not rec["viol"], rec["viol"][:3]
     assert rec["bv"] > 2000 and rec["tri"] > 50
     assert rec["bv_ok"] >= 0.99 * rec["bv"], rec
+    assert rec["bv_lane_ok"] >= 0.99 * rec["bv"], rec
     assert rec["tri_ok"] >= 0.3 * rec["tri"], rec
 
 
@@ -141,3 +149,27 @@ def test_rect_cases_lane_parallel_match_sequential(fc):
         assert tab[:4].tobytes() == out[4:8].tobytes() and tab[4] == out[8], i
         cases.add(int(out[8]))
     assert cases == set(range(-1, 16)), sorted(cases)
+
+
+def test_rect_dist_one_lane_matches_sequential(fc):
+    """rect_dist_lane (the speculative engine's RectDist: the cases in order
+    through one code path) against the sequential rect_dist and the
+    reference's RectDist outputs, bit for bit, over every case and the tail."""
+    from c2a_testutil import GOLDEN
+
+    fc.c2a_fc_rect_one_lane.argtypes = [C.c_void_p] * 5
+    z = np.load(os.path.join(GOLDEN, "geometry_ref.npz"))
+    out = np.zeros(8)
+    for i in range(len(z["rect_d"])):
+        fc.c2a_fc_rect_one_lane(_p(z["Rab"][i]), _p(z["Tab"][i]), _p(z["a"][i]), _p(z["b"][i]), _p(out))
+        assert out[4].tobytes() == np.float64(z["rect_d"][i]).tobytes(), i
+        assert out[0:4].tobytes() == out[4:8].tobytes(), i
+    rng = np.random.default_rng(8)
+    Rs = workloads.random_rotations(rng, 20000).reshape(-1, 9)
+    for i in range(20000):
+        R = Rs[i] if i % 5 else np.round(Rs[i] * 2) / 2
+        T = rng.normal(size=3) * rng.choice([0.01, 0.3, 2.0])
+        a = rng.uniform(0, 1, 2) * (rng.random(2) > 0.05)
+        b = rng.uniform(0, 1, 2) * (rng.random(2) > 0.05)
+        fc.c2a_fc_rect_one_lane(_p(R), _p(T), _p(a), _p(b), _p(out))
+        assert out[0:4].tobytes() == out[4:8].tobytes(), i
