@@ -100,6 +100,7 @@ struct SpecMinCand {
  * replay stack follow it (spec_shared_bytes) */
 struct SpecShared {
     int32_t nrec, nfree, qhead, qcount;
+    int32_t bad, pad_[3]; /* a checked build's first failed index check (site code), else 0 */
     uint32_t qref[kSpecQueue];
     uint32_t qgen[kSpecQueue];
     uint32_t cref[kSpecSlots];
@@ -150,7 +151,24 @@ struct SpecCtx {
     int overflow; /* 0, or why the step gave up (a code for the status word) */
 };
 
-C2A_KDEV SpecEnt &spec_ent(const SpecCtx &c, uint32_t ref) { return c.rec[ref >> 1].ent[ref & 1]; }
+/* Checked builds (C2A_SPEC_CHECK) verify every record reference and node or
+ * triangle index before use; a failure records a site code, the access goes
+ * to index 0 instead and the step ends with a status. */
+#ifdef C2A_SPEC_CHECK
+#define C2A_SPEC_OK(c, cond, site) ((cond) ? true : ((c).sh->bad == 0 ? ((c).sh->bad = (site)) : 0, false))
+#else
+#define C2A_SPEC_OK(c, cond, site) true
+#endif
+
+C2A_KDEV SpecEnt &spec_ent(const SpecCtx &c, uint32_t ref)
+{
+    if (!C2A_SPEC_OK(c, (int)(ref >> 1) < c.nrec, 10)) ref = 0;
+    return c.rec[ref >> 1].ent[ref & 1];
+}
+C2A_KDEV bool spec_pair_ok(const SpecCtx &c, const Query &q, int b1, int b2, int site)
+{
+    return C2A_SPEC_OK(c, b1 >= 0 && b1 < q.A->num_nodes && b2 >= 0 && b2 < q.B->num_nodes, site);
+}
 
 C2A_KDEV void spec_layout(SpecCtx &c, unsigned char *smem, unsigned char *gmem, int nrec)
 {
@@ -178,6 +196,7 @@ C2A_KDEV void spec_reset(SpecCtx &c, int nrec, int lane)
         c.sh->nfree = nrec;
         c.sh->qhead = 0;
         c.sh->qcount = 0;
+        c.sh->bad = 0;
     }
     __syncwarp();
 }
@@ -261,7 +280,8 @@ C2A_KDEV void spec_make_exact(const Query &q, SpecCtx &c, uint32_t ref, int lane
 #pragma unroll
     for (int i = 0; i < 9; i++) PR.m[i] = c.g[r].R[i];
     PT = v3(c.g[r].T[0], c.g[r].T[1], c.g[r].T[2]);
-    const int b1 = e.b1, b2 = e.b2;
+    int b1 = e.b1, b2 = e.b2;
+    if (!spec_pair_ok(c, q, b1, b2, 11)) b1 = b2 = 0;
     child_transform(q, c.rec[r].side, b1, b2, PR, PT, R, T);
     double d, m;
     child_test_x(q, b1, b2, R, T, d, m, lane);
@@ -283,6 +303,7 @@ C2A_KDEV void spec_exact_distance(Query &q, SpecCtx &c, int lane)
 {
     if (c.dist_exact) return;
     C2A_WSTAT(q, ST_S_DISTX, 1);
+    if (!spec_pair_ok(c, q, c.dist_b1, c.dist_b2, 12)) c.dist_b1 = c.dist_b2 = 0;
     const int fc1 = __ldg(&q.A->nodes[c.dist_b1].first_child), fc2 = __ldg(&q.B->nodes[c.dist_b2].first_child);
     V3 p, qq;
     TriFeat f;
@@ -410,7 +431,8 @@ C2A_KDEV void spec_leaf(Query &q, SpecCtx &c, uint32_t ref, int lane)
 {
     q.ntri++;
     const SpecEnt &e = spec_ent(c, ref);
-    const int b1 = e.b1, b2 = e.b2;
+    int b1 = e.b1, b2 = e.b2;
+    if (!spec_pair_ok(c, q, b1, b2, 13)) b1 = b2 = 0;
     const uint16_t fl = e.flags;
     if (fl & SF_LEXACT) { /* the lane computed it in FP64: the reference's comparison directly */
         const double dTri = c.g[ref >> 1].tx[ref & 1], mint = c.g[ref >> 1].tm[ref & 1];
@@ -642,8 +664,10 @@ C2A_KDEV int spec_collect(Query &q, SpecCtx &c, uint32_t due)
 C2A_KDEV void spec_leaf_task(const Query &q, SpecCtx &sc, uint32_t ref)
 {
     SpecEnt &e = spec_ent(sc, ref);
-    const int b1 = e.b1, b2 = e.b2;
-    const int ia = -__ldg(&q.A->nodes[b1].first_child) - 1, ib = -__ldg(&q.B->nodes[b2].first_child) - 1;
+    int b1 = e.b1, b2 = e.b2;
+    if (!spec_pair_ok(sc, q, b1, b2, 14)) b1 = b2 = 0;
+    int ia = -__ldg(&q.A->nodes[b1].first_child) - 1, ib = -__ldg(&q.B->nodes[b2].first_child) - 1;
+    if (!C2A_SPEC_OK(sc, ia >= 0 && ia < q.A->num_tris && ib >= 0 && ib < q.B->num_tris, 15)) ia = ib = 0;
 #ifdef C2A_SPEC_FP64
     {
         V3 p, qq;
@@ -788,7 +812,8 @@ C2A_KDEV void spec_expand(const Query &q, SpecCtx &c, int ncand, const M3 &Rroot
         const SpecEnt &e = spec_ent(c, ref);
         b1 = e.b1;
         b2 = e.b2;
-        const int pr = (int)(ref >> 1), side = c.rec[pr].side;
+        if (!spec_pair_ok(c, q, b1, b2, 16)) b1 = b2 = 0;
+        const int pr = (int)(ref >> 1) < c.nrec ? (int)(ref >> 1) : 0, side = c.rec[pr].side;
         M3 PR;
 #pragma unroll
         for (int i = 0; i < 9; i++) PR.m[i] = c.g[pr].R[i];
@@ -830,7 +855,8 @@ C2A_KDEV void spec_expand(const Query &q, SpecCtx &c, int ncand, const M3 &Rroot
     const int fc1 = __ldg(&q.A->nodes[b1].first_child), fc2 = __ldg(&q.B->nodes[b2].first_child);
     int side, a1, a2, c1, c2;
     split_pair(q, b1, b2, fc1, fc2, side, a1, a2, c1, c2);
-    const int x1 = sub ? c1 : a1, x2 = sub ? c2 : a2;
+    int x1 = sub ? c1 : a1, x2 = sub ? c2 : a2;
+    if (!spec_pair_ok(c, q, x1, x2, 17)) x1 = x2 = 0;
     EFCtx ec{!q.shadows_ok};
     const M3T<EF> Re = ef_m3(R, ec);
     const V3T<EF> Te = ef_v3(T, ec);
@@ -966,6 +992,10 @@ C2A_KDEV void spec_dfs(Query &q, const M3 &Rroot, V3 Troot, SpecCtx &c, int lane
     for (int round = 0;; round++) {
         C2A_WCLOCK(t0);
         const uint32_t due = spec_replay(q, c, lane);
+        if (c.sh->bad) {
+            c.overflow = 16 + c.sh->bad;
+            break;
+        }
         C2A_WCLOCK(t1);
         C2A_WSTAT(q, ST_S_CYC_REPLAY, t1 - t0);
         if (due == kSpecNone || c.overflow) break;
@@ -993,6 +1023,10 @@ C2A_KDEV void spec_dfs(Query &q, const M3 &Rroot, V3 Troot, SpecCtx &c, int lane
         __syncwarp();
         C2A_WCLOCK(t3);
         C2A_WSTAT(q, ST_S_CYC_EXPAND, t3 - t2);
+        if (c.sh->bad) { /* a checked build found an index out of range */
+            c.overflow = 16 + c.sh->bad;
+            break;
+        }
         /* the due pair's task must be there now, or the replay would ask again */
         if (due != kSpecRoot) {
             const SpecEnt &e = spec_ent(c, due);
