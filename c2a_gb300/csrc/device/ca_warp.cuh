@@ -38,15 +38,23 @@ namespace c2a {
 constexpr unsigned kWFull = 0xffffffffu;
 
 /* The warp-uniform state (the query, the speculative engine's bookkeeping)
- * is written by every lane with the same value; the warp executes that code
- * converged.  A host emulation of the warp, whose lanes do not run in
- * lockstep, replaces these two: a per-lane query copy, and writes fenced by
- * warp barriers so that no lane reads a location while another writes it. */
+ * is written by every lane with the same value.  The speculative engine's
+ * shared writes go through C2A_WSET, which fences each write with warp
+ * barriers, so no lane reads a location while another lane writes it even
+ * where the lanes do not run converged; the warp kernel's query updates
+ * rely on the warp executing that code converged.  A host emulation of the
+ * warp replaces the query reference with a per-lane copy. */
 #ifndef C2A_WARP_QUERY
 #define C2A_WARP_QUERY(sh) ((sh).q)
 #endif
 #ifndef C2A_WSET
-#define C2A_WSET(dst, v) ((dst) = (v))
+#define C2A_WSET(dst, v)                                                                                           \
+    do {                                                                                                           \
+        auto wset_v_ = (v);                                                                                        \
+        __syncwarp();                                                                                              \
+        (dst) = wset_v_;                                                                                           \
+        __syncwarp();                                                                                              \
+    } while (0)
 #endif
 
 /* 1: node-pair and leaf tests through the certified FP32 filter (FP64 only

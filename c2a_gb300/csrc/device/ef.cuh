@@ -172,6 +172,21 @@ struct EFCtx {
 #define C2A_EF_FAIL(c, line) ((c).bad = true)
 #endif
 
+/* Device fast paths of the quotient and the square root.  They use CUDA's
+ * approximate intrinsics within their documented accuracy: __fdividef(x, y)
+ * is within 2 ulp of x / y for 2^-126 <= |y| <= 2^126, rsqrtf(x) within 2
+ * ulp of 1 / sqrt(x).  Each approximation error enters e with a margin
+ * (2^-21 relative, i.e. 4 ulp), and the propagated part is rounded upwards
+ * through an inflation by 1 + 2^-20; outside the guarded ranges the exact
+ * directed-rounding forms below are used. */
+#if defined(__CUDA_ARCH__) && !defined(C2A_EF_PRECISE)
+#define C2A_EF_FAST 1
+#define C2A_EF_ULP4 4.76837158e-07f  /* 2^-21 */
+#define C2A_EF_INFL 1.00000095f      /* 1 + 2^-20 */
+#define C2A_EF_DEFL 0.99999905f      /* 1 - 2^-20 */
+C2A_EFI bool ef_fast_range(float x) { return fabsf(x) >= 1.0e-30f && fabsf(x) <= 1.0e30f; }
+#endif
+
 C2A_EFI EF ef_div(EF a, EF b, EFCtx &c)
 {
     const float den = ef_rd_sub(fabsf(b.v), b.e);
@@ -179,6 +194,18 @@ C2A_EFI EF ef_div(EF a, EF b, EFCtx &c)
         C2A_EF_FAIL(c, __LINE__);
         return EF{0.0f, 0.0f};
     }
+#ifdef C2A_EF_FAST
+    if (ef_fast_range(b.v) && ef_fast_range(den) && fabsf(a.v) <= 1.0e30f && a.e <= 1.0e30f) {
+        const float v = __fdividef(a.v, b.v);
+        if (a.v == 0.0f || ef_fast_range(v)) {
+            /* |a.v / b.v| <= |v| (1 + 2^-21) */
+            const float num = ef_ru_add(a.e, ef_ru_mul(ef_ru_mul(fabsf(v), 1.00000048f), b.e));
+            float s = __fmul_ru(__fdividef(num, den), C2A_EF_INFL);
+            s = ef_ru_add(s, ef_ru_mul(fabsf(v), C2A_EF_ULP4));
+            if (s == s && s <= 1.0e30f) return EF{v, ef_round_err(v, s)};
+        }
+    }
+#endif
     const float v = a.v / b.v;
     const float num = ef_ru_add(a.e, ef_ru_mul(ef_ru_mul(fabsf(v), 1.00000024f), b.e));
     float s = efr_div_ru(num, den);
@@ -189,6 +216,22 @@ C2A_EFI EF ef_div(EF a, EF b, EFCtx &c)
 C2A_EFI EF ef_sqrt(EF a)
 {
     const float x = a.v > 0.0f ? a.v : 0.0f;
+#ifdef C2A_EF_FAST
+    if ((x == 0.0f || ef_fast_range(x)) && a.e <= 1.0e30f) {
+        const float v = x == 0.0f ? 0.0f : x * rsqrtf(x); /* within 2.5 ulp of sqrt(x) */
+        const float lo = ef_rd_sub(a.v, a.e);
+        float s;
+        if (lo > 0.0f && ef_fast_range(lo)) { /* e / (sqrt(x) + sqrt(lo)) */
+            const float den = __fmul_rd(efr_add_rd(v, lo * rsqrtf(lo)), 0.9999981f);
+            s = __fmul_ru(__fdividef(a.e, den), C2A_EF_INFL);
+        } else { /* sqrt(x + e) */
+            const float t = ef_ru_add(x, a.e);
+            s = t == 0.0f ? 0.0f : __fmul_ru(t * rsqrtf(t), 1.0000019f);
+        }
+        s = ef_ru_add(s, ef_ru_mul(v, C2A_EF_ULP4));
+        if (s == s && s <= 1.0e30f) return EF{v, ef_round_err(v, s)};
+    }
+#endif
     const float v = sqrtf(x);
     const float lo = ef_rd_sub(a.v, a.e);
     float s;

@@ -272,11 +272,11 @@ def main():
     lw("        const int t2 = c2.bad ? -1 : k2, t3 = c3.bad ? -1 : k3;")
     lw("        int u1 = 1, u2 = 1;")
     lw("        if (t2 != 1) {")
-    lw("            const bool i1 = in_slab(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], s1[6], ci1);")
+    lw("            const bool i1 = in_slab_inl(s1[0], s1[1], s1[2], s1[3], s1[4], s1[5], s1[6], ci1);")
     lw("            u1 = ci1.bad ? -1 : i1;")
     lw("        }")
     lw("        if (t3 != 1) {")
-    lw("            const bool i2 = in_slab(s2[0], s2[1], s2[2], s2[3], s2[4], s2[5], s2[6], ci2);")
+    lw("            const bool i2 = in_slab_inl(s2[0], s2[1], s2[2], s2[3], s2[4], s2[5], s2[6], ci2);")
     lw("            u2 = ci2.bad ? -1 : i2;")
     lw("        }")
     lw("        const int hit = rc_and3(rc_and3(t0, t1), rc_and3(rc_or3(t2, u1), rc_or3(t3, u2)));")
@@ -301,7 +301,7 @@ def main():
     lw("        break;")
     lw("    }")
     lw("    T t, u;")
-    lw("    edge_params(t, u, e[0], e[1], e[2], e[3], e[4], ctx);")
+    lw("    edge_params_inl(t, u, e[0], e[1], e[2], e[3], e[4], ctx);")
     lw("    const T Px = px == 0 ? a[0] : px == 1 ? a[1] : px == 4 ? t : zero;")
     lw("    const T Py = py == 0 ? a[0] : py == 1 ? a[1] : py == 4 ? t : zero;")
     lw("    const V3T<T> P = v3t<T>(Px, Py, zero);")

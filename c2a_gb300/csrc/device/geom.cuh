@@ -202,7 +202,7 @@ C2A_DEV V3 v3(double x, double y, double z) { return V3{x, y, z}; }
 /* ------------------------------------------------------------- RectDist */
 
 template <class T, class C>
-C2A_NOINL void edge_params(T &t, T &u, T a, T b, T AdB, T AdT, T BdT, C &ctx)
+C2A_DEV void edge_params_inl(T &t, T &u, T a, T b, T AdB, T AdT, T BdT, C &ctx)
 {
     const T zero = K(0.0);
     T denom = K(1.0) - (AdB) * (AdB);
@@ -219,7 +219,7 @@ C2A_NOINL void edge_params(T &t, T &u, T a, T b, T AdB, T AdT, T BdT, C &ctx)
 }
 
 template <class T, class C>
-C2A_NOINL bool in_slab(T a, T b, T AnB, T AnT, T AdB, T AdT, T BdT, C &ctx)
+C2A_DEV bool in_slab_inl(T a, T b, T AnB, T AnT, T AdB, T AdT, T BdT, C &ctx)
 {
     const T zero = K(0.0);
     if (LT(abs_c(AnB), K(1e-7))) return false;
@@ -228,6 +228,18 @@ C2A_NOINL bool in_slab(T a, T b, T AnB, T AnT, T AdB, T AdT, T BdT, C &ctx)
     T v = t * AdB - BdT;
     if (GT(AnB, zero)) return GT(v, (u + K(1e-7)));
     return LT(v, (u - K(1e-7)));
+}
+
+/* the out-of-line forms the sequential rect_dist calls from its sixteen cases */
+template <class T, class C>
+C2A_NOINL void edge_params(T &t, T &u, T a, T b, T AdB, T AdT, T BdT, C &ctx)
+{
+    edge_params_inl(t, u, a, b, AdB, AdT, BdT, ctx);
+}
+template <class T, class C>
+C2A_NOINL bool in_slab(T a, T b, T AnB, T AnT, T AdB, T AdT, T BdT, C &ctx)
+{
+    return in_slab_inl(a, b, AnB, AnT, AdB, AdT, BdT, ctx);
 }
 
 /* Q = Tab + Rab[:,cb] qb + Rab[:,cu] u, evaluated as (Tab + R qb) + R u */
