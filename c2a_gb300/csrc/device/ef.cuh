@@ -242,8 +242,15 @@ C2A_EFI EF ef_sqrt(EF a)
 
 C2A_EFI EF ef_abs(EF a) { return EF{fabsf(a.v), a.e}; }
 C2A_EFI EF ef_max0(EF a) { return EF{a.v > 0.0f ? a.v : 0.0f, a.e}; }
+/* if (x < lo) x = lo; else if (x > hi) x = hi.  Where the FP64 comparisons
+ * are certain, the FP64 result is exactly that bound or x, so the result
+ * carries that operand's own error (an exact bound stays exact, and later
+ * comparisons against it decide); otherwise every operand's error. */
 C2A_EFI EF ef_clamp(EF x, EF lo, EF hi)
 {
+    const float xl = ef_rd_sub(x.v, x.e), xh = ef_ru_add(x.v, x.e);
+    if (xh < ef_rd_sub(lo.v, lo.e)) return lo;                                 /* x < lo certainly */
+    if (xl >= ef_ru_add(lo.v, lo.e) && xl > ef_ru_add(hi.v, hi.e)) return hi; /* not below lo, above hi */
     float v = x.v < lo.v ? lo.v : x.v;
     v = v > hi.v ? hi.v : v;
     return EF{v, ef_emax(x.e, ef_emax(lo.e, hi.e))};
