@@ -42,6 +42,12 @@ METRIC = "CCD queries/s on 1 GB300: learned+batched vs plain GPU CA at equal TOC
 UNIT = "queries/s"
 NODE_BYTES = 208   # FP64 node fields a BV test reads (R, Tr, l, r, angularRadius, R_loc, first_child)
 TRI_BYTES = 144    # two triangles (9 doubles each) per triangle test
+# FP64 flops (add/sub, mul, div, sqrt) of the reference's algorithm per unit of work, counted by
+# oracle/flop_count.cpp over 1,024 evenly strided queries of this batch: a node-pair test (half an
+# expansion: child transform, RSS distance, both motion bounds, descent test) and a leaf triangle
+# test (its triangle-level CA iterations included); tests/test_flop_count.py re-counts them
+F_BV = 233.6
+F_TRI = 353.4
 CONTACT_SLOTS = 64
 REFERENCE_SAMPLE = 16384  # queries per step of the CPU arms (evenly strided over the batch)
 
@@ -183,6 +189,7 @@ def run_reference(args, rank, world):
 
 
 ENGINES = {"auto": 0, "warp": 1, "batched": 2, "thread": 3, "spec": 4}
+ENGINE_OF = {"auto": "warp"}  # what ENGINE_AUTO runs in REFERENCE mode
 KERNELS = {("reference", "auto"): "c2a_solve_warp_kernel", ("reference", "warp"): "c2a_solve_warp_kernel",
            ("reference", "spec"): "c2a_solve_spec_kernel",
            ("reference", "thread"): "c2a_solve_kernel", ("canonical", "auto"): "c2a_canonical_kernel",
@@ -385,33 +392,33 @@ def main():
         raise RuntimeError("a query reported a failure status")
     value = n * world * args.steps / (total_ms / 1000.0)
 
-    # roofline of the CA kernel: algorithmic node/triangle bytes per launch / launch time
+    # roofline of the CA kernel on its binding resource, the FP64 pipe: the algorithm's flops per launch
+    # (per-unit counts x the launch's node-pair and triangle tests) over the launch time, against the FP64
+    # peak measured now on this GPU; the HBM view beside it (the trees stay in L2)
     bv = int(res["num_bv_tests"].sum())
     tri = int(res["num_tri_tests"].sum())
-    alg_bytes = bv * NODE_BYTES + tri * TRI_BYTES
     launch_s = (total_ms / args.steps) / 1000.0
+    alg_flops = bv * F_BV + tri * F_TRI
+    fma_peak, add_peak = api.fp64_peak(local)
+    achieved = alg_flops / launch_s / 1e9
+    alg_bytes = bv * NODE_BYTES + tri * TRI_BYTES
     peaks = measured_peaks()
-    peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if peak else "fallback"
-    peak = peak or 6800.0
-    achieved = alg_bytes / launch_s / 1e9
-    prof = profile_traffic()
-    traffic = None
-    if prof and prof.get("dram_bytes_per_query"):
-        traffic = float(prof["dram_bytes_per_query"]) * n
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": peak_src, "kernel": KERNELS.get((args.mode, args.engine)),
-                "algorithmic_bytes_per_launch": alg_bytes, "num_bv_tests": bv, "num_tri_tests": tri,
-                "note": "not HBM-bound (the trees stay in L2): each query is a dependent chain of FP64 node-pair "
-                        "tests whose correctly rounded divisions and square roots set the latency of an "
-                        "expansion at 8 warps per SM; the batch's makespan is set by its heaviest queries "
-                        "(warp slots busy 63 % of the time) -- see fp64_pipe and profiles/"}
-    if prof and prof.get("fp64_pipe_active_pct") is not None:
-        roofline["fp64_pipe"] = {"active_pct_of_peak": prof["fp64_pipe_active_pct"],
-                                 "fp64_share_of_instructions": (prof["inst_executed_fp64"] / prof["inst_executed"]
-                                                                if prof.get("inst_executed") else None),
-                                 "warp_slot_utilization_full_batch": prof.get("full_batch_warp_slot_utilization"),
-                                 "source": prof.get("source", "profiles")}
+    hbm_peak = peaks.get("hbm_gbs")
+    hbm_src = "measured (MEASURED_PEAKS.json)" if hbm_peak else "fallback"
+    hbm_peak = hbm_peak or 6800.0
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fma_peak / 1e9, "unit": "GFLOP/s",
+                "frac": achieved / (fma_peak / 1e9), "traffic": None,
+                "peak_source": "measured in this run: c2a_probe_fp64_peak (FP64 FMA chains on every SM, best of 5)",
+                "peak_unfused": add_peak / 1e9, "frac_of_unfused": achieved / (add_peak / 1e9),
+                "kernel": KERNELS.get((args.mode, args.engine)),
+                "flops_per_bv_test": F_BV, "flops_per_tri_test": F_TRI, "algorithmic_flops_per_launch": alg_flops,
+                "num_bv_tests": bv, "num_tri_tests": tri,
+                "hbm": {"achieved": alg_bytes / launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                        "frac": alg_bytes / launch_s / 1e9 / hbm_peak, "peak_source": hbm_src,
+                        "algorithmic_bytes_per_launch": alg_bytes},
+                "note": "traffic: not measured in this run (ncu DRAM bytes of a small capture are in profiles/); "
+                        "peak_unfused: the same pipe issuing one add per instruction, the ceiling of code "
+                        "compiled without contraction as the reference's is"}
 
     e2e = None
     if not args.no_e2e:

@@ -30,6 +30,12 @@ CONTACT_DTYPE = np.dtype([("type_a", np.int32), ("type_b", np.int32), ("fid_a", 
 DISTANCE_DTYPE = np.dtype([("distance", np.float64), ("p1", np.float64, (3,)), ("p2", np.float64, (3,)),
                            ("tri_a", np.int32), ("tri_b", np.int32), ("status", np.int32), ("pad", np.int32)],
                           align=True)
+TOLERANCE_DTYPE = np.dtype([("closer", np.int32), ("status", np.int32), ("distance", np.float64),
+                            ("p1", np.float64, (3,)), ("p2", np.float64, (3,)), ("num_bv_tests", np.int64),
+                            ("num_tri_tests", np.int64)], align=True)
+COLLIDE_DTYPE = np.dtype([("num_pairs", np.int32), ("status", np.int32), ("num_bv_tests", np.int64),
+                          ("num_tri_tests", np.int64)], align=True)
+assert TOLERANCE_DTYPE.itemsize == 80 and COLLIDE_DTYPE.itemsize == 24
 assert QUERY_DTYPE.itemsize == 400 and RESULT_DTYPE.itemsize == 264 and CONTACT_DTYPE.itemsize == 104
 assert DISTANCE_DTYPE.itemsize == 72
 
@@ -41,11 +47,15 @@ NOALLOC_MAX_MODELS = 120  # C2A_NOALLOC_MAX_MODELS
 
 # every extern "C" symbol of include/c2a_gb300.h
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
-               "c2a_model_info", "c2a_model_download", "c2a_model_free", "c2a_solve_batch",
+               "c2a_model_info", "c2a_model_download", "c2a_model_download_obb", "c2a_model_free",
+               "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
                "c2a_distance_batch", "c2a_solve_batch_hinted", "c2a_solve_batch_ordered",
-               "c2a_solve_batch_ordered_host",
+               "c2a_solve_batch_ordered_host", "c2a_tolerance_batch", "c2a_collide_batch",
                "c2a_motion_setup", "c2a_motion_integrate"]
+
+# include/c2a_probe.h
+PROBE_SYMBOLS = ["c2a_probe_fp64_peak"]
 
 
 class Params(C.Structure):
@@ -108,6 +118,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_model_build": ([vp, i32, vp, vp, vp, C.POINTER(i32)], i32),
         "c2a_model_info": ([vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
         "c2a_model_download": ([vp, i32, vp, vp, vp, vp, vp], i32),
+        "c2a_model_download_obb": ([vp, i32, vp], i32),
         "c2a_model_free": ([vp, i32], i32),
         "c2a_solve_batch": ([vp, vp, i32, C.POINTER(Params), vp, vp], i32),
         "c2a_solve_batch_device": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp], i32),
@@ -117,6 +128,9 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_distance_batch": ([vp, vp, i32, vp], i32),
         "c2a_solve_batch_ordered": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp, vp], i32),
         "c2a_solve_batch_ordered_host": ([vp, vp, i32, C.POINTER(Params), vp, vp, vp], i32),
+        "c2a_tolerance_batch": ([vp, vp, i32, vp, vp], i32),
+        "c2a_collide_batch": ([vp, vp, i32, i32, i32, vp, vp], i32),
+        "c2a_probe_fp64_peak": ([C.c_int, C.c_int, C.POINTER(dbl), C.POINTER(dbl)], i32),
         "c2a_motion_setup": ([vp, vp, vp, vp, vp], i32),
         "c2a_motion_integrate": ([vp, vp, vp, vp, dbl, vp, vp, vp], i32),
     }
@@ -126,6 +140,15 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         f.restype = res
     _LIB = lib
     return lib
+
+
+def fp64_peak(device: int = 0, repeats: int = 5) -> tuple[float, float]:
+    """The FP64 pipe's measured peak on ``device``: (fused multiply-add flop/s,
+    plain-addition flop/s), the best of ``repeats`` launches each."""
+    lib = load()
+    f, a = C.c_double(), C.c_double()
+    _check(lib.c2a_probe_fp64_peak(device, repeats, C.byref(f), C.byref(a)), "c2a_probe_fp64_peak")
+    return f.value, a.value
 
 
 def status_str(s: int) -> str:
@@ -225,6 +248,13 @@ class Context:
                "c2a_model_download")
         return f, fc, tv, tid, tidx
 
+    def download_obb(self, mid: int) -> np.ndarray:
+        """(nodes, 6): each node's OBB centre in its parent's frame and half extents."""
+        _, nn, _ = self.model_info(mid)
+        o = np.zeros((nn, 6))
+        _check(self.lib.c2a_model_download_obb(self.h, mid, _ptr(o)), "c2a_model_download_obb")
+        return o
+
     def free_model(self, mid: int):
         _check(self.lib.c2a_model_free(self.h, mid), "c2a_model_free")
 
@@ -257,6 +287,33 @@ class Context:
         if check:
             _check(s, "c2a_distance_batch")
         return res
+
+    def tolerance(self, qint: np.ndarray, poses: np.ndarray, tolerance, check: bool = True) -> np.ndarray:
+        """C2A_Tolerance (qsize 2) for a batch: model_a at pose[0:12], model_b at
+        pose[24:36]; tolerance is a scalar or one per query; TOLERANCE_DTYPE rows."""
+        q = make_queries(qint, poses)
+        n = len(q)
+        tol = np.ascontiguousarray(np.broadcast_to(np.asarray(tolerance, dtype=np.float64), (n,)))
+        res = np.zeros(n, dtype=TOLERANCE_DTYPE)
+        s = self.lib.c2a_tolerance_batch(self.h, _ptr(q), n, _ptr(tol), _ptr(res))
+        if check:
+            _check(s, "c2a_tolerance_batch")
+        return res
+
+    def collide(self, qint: np.ndarray, poses: np.ndarray, flag: int = 1, pairs_per_query: int = 256,
+                check: bool = True):
+        """C2A_Collide for a batch: (COLLIDE_DTYPE rows, pairs (n, pairs_per_query,
+        2) caller triangle ids in visiting order, the first min(num_pairs, slots)
+        of each row valid)."""
+        q = make_queries(qint, poses)
+        n = len(q)
+        res = np.zeros(n, dtype=COLLIDE_DTYPE)
+        pairs = np.zeros((n, max(1, pairs_per_query), 2), dtype=np.int32)
+        s = self.lib.c2a_collide_batch(self.h, _ptr(q), n, int(flag), int(pairs_per_query), _ptr(res),
+                                       _ptr(pairs) if pairs_per_query > 0 else None)
+        if check:
+            _check(s, "c2a_collide_batch")
+        return res, pairs[:, :pairs_per_query]
 
     def solve_ordered_host(self, qint: np.ndarray, poses: np.ndarray, params: dict, d_order: int,
                            contacts_per_query: int = 64, check: bool = True):

@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libc2a_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["c2a_abi.cu", "k_thread.cu", "k_warp.cu", "k_spec.cu", "k_front.cu", "c2a_wave.cu", "mlp.cu"]
+CUDA_SOURCES = ["c2a_abi.cu", "k_thread.cu", "k_warp.cu", "k_spec.cu", "k_front.cu", "k_static.cu", "c2a_wave.cu", "mlp.cu", "probe.cu"]
 HOST_SOURCES = ["host/bvh_build.cpp", "host/c2a_api.cpp"]
 HOST_FLAGS = "-fPIC,-O2,-ffp-contract=off,-fno-fast-math,-Wall"
 

@@ -38,6 +38,7 @@ struct ModelSlot {
     TriRec *d_tris = nullptr;
     NodeShadow *d_snodes = nullptr;
     TriShadow *d_stris = nullptr;
+    ObbRec *d_obbs = nullptr;
     bool live = false;
 };
 
@@ -49,6 +50,7 @@ DevModel dev_model_of(const ModelSlot &s)
     m.tris = s.d_tris;
     m.snodes = s.d_snodes;
     m.stris = s.d_stris;
+    m.obbs = s.d_obbs;
     m.num_tris = s.live ? (int32_t)s.host.tris.size() : 0;
     m.num_nodes = s.live ? (int32_t)s.host.nodes.size() : 0;
     m.depth = s.host.depth;
@@ -62,6 +64,8 @@ void free_slot(ModelSlot &s)
     if (s.d_tris) cudaFree(s.d_tris);
     if (s.d_snodes) cudaFree(s.d_snodes);
     if (s.d_stris) cudaFree(s.d_stris);
+    if (s.d_obbs) cudaFree(s.d_obbs);
+    s.d_obbs = nullptr;
     s.d_nodes = nullptr;
     s.d_tris = nullptr;
     s.d_snodes = nullptr;
@@ -411,6 +415,10 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
     if (e == cudaSuccess) e = cudaMalloc(&slot.d_tris, sizeof(TriRec) * nt);
     if (e == cudaSuccess) e = cudaMalloc(&slot.d_snodes, sizeof(NodeShadow) * nn);
     if (e == cudaSuccess) e = cudaMalloc(&slot.d_stris, sizeof(TriShadow) * nt);
+    if (e == cudaSuccess) e = cudaMalloc(&slot.d_obbs, sizeof(ObbRec) * nn);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_obbs, slot.host.obbs.data(), sizeof(ObbRec) * nn, cudaMemcpyHostToDevice,
+                            ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(slot.d_nodes, slot.host.nodes.data(), sizeof(NodeRec) * nn, cudaMemcpyHostToDevice,
                             ctx->stream);
@@ -475,6 +483,18 @@ c2a_status c2a_model_download(c2a_context *ctx, int32_t id, double *node_f, int3
         if (tri_ids) tri_ids[i] = t.id;
         if (tri_vidx)
             for (int k = 0; k < 3; k++) tri_vidx[3 * i + k] = t.idx[k];
+    }
+    return C2A_OK;
+}
+
+c2a_status c2a_model_download_obb(c2a_context *ctx, int32_t id, double *obb)
+{
+    if (!ctx || !obb) return C2A_ERR_INVALID_ARGUMENT;
+    if (id < 0 || id >= (int32_t)ctx->models.size() || !ctx->models[id].live) return C2A_ERR_BAD_MODEL;
+    const BuiltModel &m = ctx->models[id].host;
+    for (size_t i = 0; i < m.obbs.size(); i++) {
+        std::memcpy(obb + 6 * i, m.obbs[i].To, sizeof(m.obbs[i].To));
+        std::memcpy(obb + 6 * i + 3, m.obbs[i].d, sizeof(m.obbs[i].d));
     }
     return C2A_OK;
 }
@@ -826,6 +846,85 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
                                                        d_contacts, d_counter);
     ctx->launches++;
     C2A_CUDA(cudaGetLastError());
+    return C2A_OK;
+}
+
+static_assert(sizeof(c2a_tolerance_result) == 80 && sizeof(c2a_collide_result) == 24, "record layouts");
+
+namespace {
+/* the host-buffer static queries: queries (and the per-query doubles) in,
+ * one launch, results (and the pairs) out */
+c2a_status static_prepare(c2a_context *ctx, const c2a_query *queries, int32_t n)
+{
+    if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
+    if (!ctx || n < 0 || (n > 0 && !queries)) return C2A_ERR_INVALID_ARGUMENT;
+    C2A_CUDA(cudaSetDevice(ctx->device));
+    c2a_status st = check_depths(ctx);
+    if (st) return st;
+    return sync_models(ctx);
+}
+} // namespace
+
+c2a_status c2a_tolerance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *tolerance,
+                               c2a_tolerance_result *results)
+{
+    if (n > 0 && (!tolerance || !results)) return C2A_ERR_INVALID_ARGUMENT;
+    if (ctx) {
+        std::lock_guard<std::mutex> lock(ctx->mu);
+        c2a_status st = static_prepare(ctx, queries, n);
+        if (st || n == 0) return st;
+        const size_t nq = (size_t)n;
+        const size_t a = ((sizeof(c2a_query) * nq + 255) / 256) * 256, b = ((sizeof(double) * nq + 255) / 256) * 256;
+        st = ensure_buf(ctx, a + b + sizeof(c2a_tolerance_result) * nq);
+        if (st) return st;
+        char *base = (char *)ctx->d_buf;
+        c2a_query *dq = (c2a_query *)base;
+        double *dt = (double *)(base + a);
+        c2a_tolerance_result *dr = (c2a_tolerance_result *)(base + a + b);
+        C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
+        C2A_CUDA(cudaMemcpyAsync(dt, tolerance, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->stream));
+        c2a_tolerance_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
+            dq, n, dt, ctx->d_models, (int)ctx->models.size(), dr);
+        ctx->launches++;
+        C2A_CUDA(cudaGetLastError());
+        C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_tolerance_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));
+        C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int32_t i = 0; i < n; i++)
+            if (results[i].status) return C2A_ERR_QUERY_FAILED;
+        return C2A_OK;
+    }
+    return C2A_ERR_INVALID_ARGUMENT;
+}
+
+c2a_status c2a_collide_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, int32_t flag,
+                             int32_t pairs_per_query, c2a_collide_result *results, int32_t *pairs)
+{
+    if (n > 0 && !results) return C2A_ERR_INVALID_ARGUMENT;
+    if (pairs_per_query < 0 || (flag != 1 && flag != 2)) return C2A_ERR_INVALID_ARGUMENT;
+    if (!ctx) return C2A_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    c2a_status st = static_prepare(ctx, queries, n);
+    if (st || n == 0) return st;
+    const size_t nq = (size_t)n, slots = pairs ? (size_t)pairs_per_query : 0;
+    const size_t a = ((sizeof(c2a_query) * nq + 255) / 256) * 256;
+    const size_t r = ((sizeof(c2a_collide_result) * nq + 255) / 256) * 256;
+    st = ensure_buf(ctx, a + r + 2 * sizeof(int32_t) * nq * slots);
+    if (st) return st;
+    char *base = (char *)ctx->d_buf;
+    c2a_query *dq = (c2a_query *)base;
+    c2a_collide_result *dr = (c2a_collide_result *)(base + a);
+    int32_t *dp = slots ? (int32_t *)(base + a + r) : nullptr;
+    C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
+    c2a_collide_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
+        dq, n, flag, ctx->d_models, (int)ctx->models.size(), (int)slots, dr, dp);
+    ctx->launches++;
+    C2A_CUDA(cudaGetLastError());
+    C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_collide_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));
+    if (slots)
+        C2A_CUDA(cudaMemcpyAsync(pairs, dp, 2 * sizeof(int32_t) * nq * slots, cudaMemcpyDeviceToHost, ctx->stream));
+    C2A_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int32_t i = 0; i < n; i++)
+        if (results[i].status & ~C2A_QUERY_CONTACT_OVERFLOW) return C2A_ERR_QUERY_FAILED;
     return C2A_OK;
 }
 

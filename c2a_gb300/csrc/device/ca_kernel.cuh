@@ -79,6 +79,7 @@ struct DevModel {
     const TriRec *tris;
     const NodeShadow *snodes;
     const TriShadow *stris;
+    const ObbRec *obbs; /* OBB per node (the static collide query) */
     int32_t num_tris;
     int32_t num_nodes;
     int32_t depth;

@@ -58,6 +58,8 @@ struct Tri {
 struct AbsNode {
     double R[3][3];
     double Tr[3];
+    double To[3]; /* OBB centre, model frame */
+    double d[3];  /* OBB half extents */
     double l[2];
     double r;
     double angR;
@@ -140,6 +142,24 @@ class Builder {
         auto X = [P](int32_t k) { return P[3 * k]; };
         auto Y = [P](int32_t k) { return P[3 * k + 1]; };
         auto Z = [P](int32_t k) { return P[3 * k + 2]; };
+
+        // the OBB in the same frame: projected extents, centre back in the model frame
+        {
+            double lox = X(0), hix = X(0), loy = Y(0), hiy = Y(0), loz = Z(0), hiz = Z(0);
+            for (int32_t i = 1; i < np; i++) {
+                if (X(i) < lox) lox = X(i);
+                else if (X(i) > hix) hix = X(i);
+                if (Y(i) < loy) loy = Y(i);
+                else if (Y(i) > hiy) hiy = Y(i);
+                if (Z(i) < loz) loz = Z(i);
+                else if (Z(i) > hiz) hiz = Z(i);
+            }
+            const double c[3] = {0.5 * (hix + lox), 0.5 * (hiy + loy), 0.5 * (hiz + loz)};
+            r_mul(b.To, b.R, c);
+            b.d[0] = 0.5 * (hix - lox);
+            b.d[1] = 0.5 * (hiy - loy);
+            b.d[2] = 0.5 * (hiz - loz);
+        }
 
         double minz = Z(0), maxz = Z(0);
         for (int32_t i = 1; i < np; i++) {
@@ -376,6 +396,7 @@ int build_rss_model(int32_t num_tris, const double *tv, const int32_t *ids, cons
     Builder(tris, nodes).run();
 
     out.nodes.assign((size_t)num_nodes, NodeRec{});
+    out.obbs.assign((size_t)num_nodes, ObbRec{});
     out.tris.assign((size_t)num_tris, TriRec{});
     out.depth = 0;
     for (int32_t i = 0; i < num_nodes; i++) {
@@ -394,6 +415,10 @@ int build_rss_model(int32_t num_tris, const double *tv, const int32_t *ids, cons
             }
         const double d[3] = {b.Tr[0] - PT[0], b.Tr[1] - PT[1], b.Tr[2] - PT[2]};
         rt_mul(o.Tr, PR, d);
+        const double *PTo = b.parent >= 0 ? nodes[b.parent].To : Z;
+        const double dO[3] = {b.To[0] - PTo[0], b.To[1] - PTo[1], b.To[2] - PTo[2]};
+        rt_mul(out.obbs[i].To, PR, dO);
+        for (int k = 0; k < 3; k++) out.obbs[i].d[k] = b.d[k];
         o.l[0] = b.l[0];
         o.l[1] = b.l[1];
         o.r = b.r;

@@ -59,7 +59,17 @@ struct alignas(16) TriShadow {
 };
 static_assert(sizeof(TriShadow) == 48, "triangle shadow must stay 48 bytes");
 
+/* The node's OBB (the static collide query's bounding volume, fitted in the
+ * RSS frame, C2A/src/C2A_BV.cpp:144-170): centre To relative to the parent
+ * (as make_parent_relative stores it) and half extents d. */
+struct alignas(16) ObbRec {
+    double To[3];
+    double d[3];
+};
+static_assert(sizeof(ObbRec) == 48, "OBB record must stay 48 bytes");
+
 struct BuiltModel {
+    std::vector<ObbRec> obbs;
     std::vector<NodeRec> nodes;
     std::vector<TriRec> tris;
     std::vector<NodeShadow> snodes;

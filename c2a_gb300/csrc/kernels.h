@@ -1,6 +1,6 @@
 /*
  * kernels.h -- the CA kernels, defined one family per translation unit
- * (k_thread.cu, k_warp.cu, k_spec.cu, k_front.cu) so they compile in
+ * (k_thread.cu, k_warp.cu, k_spec.cu, k_front.cu, k_static.cu) so they compile in
  * parallel; c2a_abi.cu launches them.
  */
 #ifndef C2A_KERNELS_H
@@ -40,5 +40,11 @@ __global__ void c2a_canonical_kernel(const c2a_query *__restrict__ queries, int 
 __global__ void c2a_distance_kernel(const c2a_query *__restrict__ queries, int n, const c2a::DevModel *__restrict__
     models, int num_models, c2a_distance_result *__restrict__ results, unsigned int *__restrict__ counter,
     c2a::Pending *__restrict__ fronts);
+
+__global__ void c2a_tolerance_kernel(const c2a_query *__restrict__ queries, int n, const double *__restrict__ tolerance,
+    const c2a::DevModel *__restrict__ models, int num_models, c2a_tolerance_result *__restrict__ results);
+__global__ void c2a_collide_kernel(const c2a_query *__restrict__ queries, int n, int flag,
+    const c2a::DevModel *__restrict__ models, int num_models, int slots, c2a_collide_result *__restrict__ results,
+    int32_t *__restrict__ pairs);
 
 #endif

@@ -160,6 +160,26 @@ typedef struct c2a_distance_result {
     int32_t pad;
 } c2a_distance_result;
 
+/* C2A_Tolerance's outputs (PQP_ToleranceResult) for one pair of placed models */
+typedef struct c2a_tolerance_result {
+    int32_t closer;        /* a triangle pair lies within the tolerance (closer_than_tolerance) */
+    int32_t status;        /* C2A_QUERY_* flags */
+    double distance;       /* that pair's distance (when closer) */
+    double p1[3];          /* its closest point on model a, model a's frame */
+    double p2[3];          /* its closest point on model b, model b's frame */
+    int64_t num_bv_tests;  /* reference counters */
+    int64_t num_tri_tests;
+} c2a_tolerance_result;
+
+/* C2A_Collide's counts (PQP_CollideResult) for one pair of placed models; the
+ * contacting triangle pairs (caller ids) go to a separate buffer */
+typedef struct c2a_collide_result {
+    int32_t num_pairs;     /* all contacting pairs found (may exceed the slots) */
+    int32_t status;        /* C2A_QUERY_* flags (CONTACT_OVERFLOW: more pairs than slots) */
+    int64_t num_bv_tests;
+    int64_t num_tri_tests;
+} c2a_collide_result;
+
 /* ---- context --------------------------------------------------------- */
 /* device >= 0: a CUDA device; device == -1: a host-only context that builds
  * and downloads models but runs no query (C2A_ERR_NO_DEVICE). */
@@ -182,6 +202,11 @@ c2a_status c2a_model_info(c2a_context *ctx, int32_t model_id, int32_t *num_tris,
  * order (9 doubles, id, 3 vertex indices). */
 c2a_status c2a_model_download(c2a_context *ctx, int32_t model_id, double *node_f, int32_t *first_child,
                               double *tri_verts, int32_t *tri_ids, int32_t *tri_vidx);
+/* The OBB of every node (the collide query's bounding volumes, fitted in the
+ * RSS frame as C2A/src/C2A_BV.cpp:144-170 does): 6 doubles per node, the
+ * centre relative to the parent's frame (make_parent_relative,
+ * C2A/src/C2A_Build.cpp:493-544) and the half extents. */
+c2a_status c2a_model_download_obb(c2a_context *ctx, int32_t model_id, double *obb);
 c2a_status c2a_model_free(c2a_context *ctx, int32_t model_id);
 
 /* ---- queries (host buffers; synchronous) ------------------------------ */
@@ -286,6 +311,24 @@ c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, 
  * o2->last_tri do.  One warp per pair walks a front of node pairs culled by
  * certified FP32 RSS bounds against the running minimum. */
 c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, c2a_distance_result *results);
+
+/* C2A_Tolerance(res, R1, T1, o1, R2, T2, o2, tolerance, 2)
+ * (C2A/src/C2A_PQP.cpp:1762-1845, C2AToleranceRecurse 1498-1603) for n
+ * pairs at once (host buffers; the call synchronises): query i places
+ * model_a by pose[0..11] and model_b by pose[24..35]; the search stops at the
+ * first triangle pair within tolerance[i] in the reference's depth-first
+ * order (closer child first).  One thread per pair, FP64. */
+c2a_status c2a_tolerance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *tolerance,
+                               c2a_tolerance_result *results);
+
+/* C2A_Collide(res, R1, T1, o1, R2, T2, o2, flag) (C2A/src/C2A_PQP.cpp:910-968,
+ * CollideRecurse 798-909) for n pairs at once (host buffers; synchronous):
+ * every triangle pair whose OBBs overlap all the way down and whose distance
+ * is zero, in visiting order, as caller triangle ids (pairs: n x
+ * pairs_per_query x 2 int32, may be NULL); flag 1 all contacts, 2 the first
+ * only (C2A_FIRST_CONTACT). */
+c2a_status c2a_collide_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, int32_t flag,
+                             int32_t pairs_per_query, c2a_collide_result *results, int32_t *pairs);
 
 /* ---- motion (host) --------------------------------------------------- */
 /* CInterpMotion_Linear constants of one object: out[0:3] axis, out[3]

@@ -16,6 +16,14 @@
 #ifndef C2A_PORT_H
 #define C2A_PORT_H
 
+/* Operation-count attribution: oracle/flop_count.cpp compiles the port with a
+ * counting double and defines this to open a scope whose arithmetic goes to
+ * bucket k (1: a node-pair expansion, 2: a leaf triangle test, 3: contact
+ * enumeration); empty everywhere else. */
+#ifndef C2A_PORT_SCOPE
+#define C2A_PORT_SCOPE(k)
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif

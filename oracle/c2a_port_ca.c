@@ -283,6 +283,7 @@ static void toc_recurse(step_state *st, const double R[3][3], const double T[3],
     int l1 = n1->first_child < 0, l2 = n2->first_child < 0;
     if (l1 && l2) {
         double p[3], q[3], dTri;
+        C2A_PORT_SCOPE(2);
         const c2a_port_tri *t1 = &st->o1->tris[-n1->first_child - 1];
         const c2a_port_tri *t2 = &st->o2->tris[-n2->first_child - 1];
         dTri = tri_distance_plain((const double(*)[3])st->R, st->T, t1, t2, p, q);
@@ -310,6 +311,7 @@ static void toc_recurse(step_state *st, const double R[3][3], const double T[3],
     {
         int a1, a2, c1, c2;
         double R1[3][3], T1[3], R2[3][3], T2[3], d1, d2, mintb, minta;
+        C2A_PORT_SCOPE(1);
         children(st, b1, b2, R, T, &a1, &a2, &c1, &c2, R1, T1, R2, T2);
         mintb = child_mint(st, (const double(*)[3])R1, T1, a1, a2, &d1);
         minta = child_mint(st, (const double(*)[3])R2, T2, c1, c2, &d2);
@@ -718,6 +720,7 @@ static void toc_recurse_translation(step_state *st, const double R[3][3], const 
     int l1 = n1->first_child < 0, l2 = n2->first_child < 0;
     if (l1 && l2) {
         double tri1[3][3], tri2[3][3];
+        C2A_PORT_SCOPE(2);
         int ia = -n1->first_child - 1, ib = -n2->first_child - 1;
         const c2a_port_tri *t1 = &st->o1->tris[ia], *t2 = &st->o2->tris[ib];
         pv_copy(tri1[0], t1->p1);
@@ -737,6 +740,7 @@ static void toc_recurse_translation(step_state *st, const double R[3][3], const 
     {
         int a1, a2, c1, c2;
         double R1[3][3], T1[3], R2[3][3], T2[3], d1, d2, minta, mintc;
+        C2A_PORT_SCOPE(1);
         children(st, b1, b2, R, T, &a1, &a2, &c1, &c2, R1, T1, R2, T2);
         d1 = d2 = 1e+30;
         minta = mintc = st->mint;
@@ -848,6 +852,7 @@ static void toc_step(step_state *st, double R1[3][3], double T1[3], double R2[3]
  * reference pushes each at the front of its list) */
 static void contact_recurse(step_state *st, const double R[3][3], const double T[3], int b1, int b2)
 {
+    C2A_PORT_SCOPE(3);
     const c2a_port_node *n1 = &st->o1->nodes[b1], *n2 = &st->o2->nodes[b2];
     int l1 = n1->first_child < 0, l2 = n2->first_child < 0;
     if (l1 && l2) {

@@ -132,6 +132,26 @@ class Port:
             raise RuntimeError(f"{bad} queries rejected by the oracle port")
         return res, con.reshape(n, max(contacts_per_query, 1))
 
+    def count_flops(self, models, qint: np.ndarray, poses: np.ndarray, params: dict) -> dict:
+        """FP64 operation counts of the port's CA path over a batch
+        (flop_count.cpp): per bucket (other, expansion, triangle test,
+        contacts) the add/sub, mul, div, sqrt and compare counts, and the
+        summed num_bv_tests / num_tri_tests."""
+        lib = C.CDLL(os.path.join(HERE, "_build", "libc2a_flops.so"))
+        lib.c2a_fc_solve.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]
+        lib.c2a_fc_solve.restype = C.c_int
+        qint = np.ascontiguousarray(qint, dtype=np.int32)
+        poses = np.ascontiguousarray(poses, dtype=np.float64)
+        ops = np.zeros((4, 5), dtype=np.int64)
+        cnt = np.zeros(2, dtype=np.int64)
+        prm = _params(params)
+        bad = lib.c2a_fc_solve(C.cast(models, C.c_void_p), len(models), _dptr(qint), _dptr(poses), len(qint),
+                               C.byref(prm), _dptr(ops), _dptr(cnt))
+        if bad:
+            raise RuntimeError(f"{bad} queries rejected by the counting port")
+        return {"ops": ops, "num_bv_tests": int(cnt[0]), "num_tri_tests": int(cnt[1])}
+
     def distance(self, models, ia: int, ib: int, R, T, seed_a: int, seed_b: int):
         """C2A_Distance (rel_err = abs_err = 0) with B placed in A's frame by (R, T):
         (distance, tri_a, tri_b) in the reference's order and tie rule."""

@@ -26,6 +26,8 @@ def test_library_exports_every_declared_symbol(lib):
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     assert sorted(api.ABI_SYMBOLS) == names
+    probe = declared_symbols("c2a_probe.h")
+    assert sorted(api.PROBE_SYMBOLS) == probe and all(hasattr(lib, n) for n in probe)
     mlp = declared_symbols("c2a_mlp.h")
     assert [n for n in mlp if not hasattr(lib, n)] == []
     assert sorted(learned.MLP_SYMBOLS) == mlp
