@@ -6,13 +6,17 @@ The `.ani` format (reader: CCDDemo/mainTorusknot.cpp:565-598): a header
 column (R[0][0] R[1][0] R[2][0] R[0][1] ...), and the three of T.
 
 The demo's queries (cb_display, CCDDemo/mainTorusknot.cpp:207-325): frame i
+(0 .. nframes - 1, the display loop's iframe)
 moves object 0 from key frame step1 to step2 (0->1 for i < 101, 101->102 for
 i < 202, else 202->203) and object 1 from its own translations at step1 and
 step2 with the rotation of its key frame i held fixed, every frame solved
 with C2A_Solve (th_ca ignored there, so tolerance 1e-4).  The demo seeds each
 frame with the triangles the previous query left in the models' last_tri
 (C2A.cpp:1175 mutates them); this library never mutates a model, so the
-replay takes explicit seeds (triangle 0 unless given).
+replay takes explicit seeds (triangle 0 unless given; the shipped scene's
+fixture records the reference's per-frame seeds).  The shipped scene: both
+objects tri_models/bunny_noholes.tri, object 0 keyed by models/torusknot1.ani,
+object 1 by models/torusknot2.ani (mainTorusknot.cpp:53-57).
 """
 from __future__ import annotations
 
@@ -61,9 +65,10 @@ def demo_steps(i: int) -> tuple[int, int, int]:
 
 def demo_queries(ani0, ani1, nframes: int | None = None, seeds=(0, 0),
                  model_a: int = 0, model_b: int = 1) -> tuple[np.ndarray, np.ndarray]:
-    """The demo's per-frame queries for frames 0 .. nframes - 2 (qint, poses)."""
+    """The demo's per-frame queries for frames 0 .. nframes - 1 (qint, poses);
+    seeds is one (seed_a, seed_b) pair for every frame or one pair per frame."""
     (R0, T0), (R1, T1) = ani0, ani1
-    n = (nframes if nframes is not None else len(R0)) - 1
+    n = nframes if nframes is not None else len(R0)
     poses = np.zeros((n, workloads.POSE_WIDTH))
     for i in range(n):
         s1, s2, s3 = demo_steps(i)
@@ -77,7 +82,8 @@ def demo_queries(ani0, ani1, nframes: int | None = None, seeds=(0, 0),
         poses[i, 45:48] = T1[s2]
     qint = np.zeros((n, 4), dtype=np.int32)
     qint[:, 0], qint[:, 1] = model_a, model_b
-    qint[:, 2], qint[:, 3] = seeds
+    sd = np.asarray(seeds, dtype=np.int32)
+    qint[:, 2:4] = sd if sd.ndim == 2 else sd[None, :]
     return qint, poses
 
 

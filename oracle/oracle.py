@@ -213,6 +213,7 @@ class Ref:
         L.c2a_ref_model_build.restype = C.c_void_p
         L.c2a_ref_model_num_nodes.argtypes = [C.c_void_p]
         L.c2a_ref_model_num_tris.argtypes = [C.c_void_p]
+        L.c2a_ref_model_last_tri.argtypes = [C.c_void_p]
         L.c2a_ref_model_dump.argtypes = [C.c_void_p] * 6
         L.c2a_ref_solve.argtypes = [C.c_void_p, C.c_void_p] + [C.c_void_p] * 8 + [C.c_int, C.c_int] + \
                                    [C.c_double] * 4 + [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
@@ -234,6 +235,10 @@ class Ref:
     @staticmethod
     def available() -> bool:
         return os.path.exists(REF_SO)
+
+    def last_tri(self, h) -> int:
+        """The model's last_tri (post-build index): the seed the demo passes next."""
+        return int(self.lib.c2a_ref_model_last_tri(h))
 
     def model(self, mesh):
         tv = mesh.tri_verts()

@@ -70,6 +70,7 @@ void *c2a_ref_model_build(int num_tris, const double *tv, const int *ids, const 
 }
 
 int c2a_ref_model_num_nodes(void *h) { return ((C2A_Model *)h)->num_bvs; }
+int c2a_ref_model_last_tri(void *h);
 int c2a_ref_model_num_tris(void *h) { return ((C2A_Model *)h)->num_tris; }
 
 // node fields the CA path reads: R(9) Tr(3) l(2) r angR Rloc(9) -> 25 doubles
@@ -110,6 +111,14 @@ static void m9(PQP_REAL R[3][3], const double *v)
 }
 
 static int tri_index(C2A_Model *m, Tri *t) { return (int)((C2A_Tri *)t - (C2A_Tri *)m->tris); }
+
+// the model's last_tri (C2A.cpp:1175 and C2A_PQP.cpp:516 move it; the demo
+// seeds each frame with it, CCDDemo/mainTorusknot.cpp:285-286)
+int c2a_ref_model_last_tri(void *h)
+{
+  C2A_Model *m = (C2A_Model *)h;
+  return tri_index(m, m->last_tri);
+}
 
 static int copy_contacts(const C2A_TimeOfContactResult &dres, ref_contact *out, int max_out)
 {

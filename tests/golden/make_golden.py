@@ -4,6 +4,7 @@ Run where the reference is compiled (``make -C oracle ref``):
 
     python tests/golden/make_golden.py            # every fixture
     python tests/golden/make_golden.py canonical  # the canonical-mode ones only
+    python tests/golden/make_golden.py demo       # the shipped demo scene only
 
 Each fixture stores its inputs (mesh vertices and faces, query poses and
 seeds, parameters) together with what the reference computed, so checking it
@@ -26,7 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from c2a_gb300 import meshes, workloads  # noqa: E402
+from c2a_gb300 import meshes, replay, workloads  # noqa: E402
 from oracle.oracle import RESULT_DTYPE, CONTACT_DTYPE, Ref, build  # noqa: E402
 
 
@@ -291,9 +292,54 @@ def static_query_fixtures(ref):
     np.savez_compressed(os.path.join(HERE, "static_queries_ref.npz"), **arrays)
 
 
+REF_DIR = os.environ.get("C2A_REF_DIR", "/root/reference")
+
+
+def demo_scene_fixture(ref):
+    """The shipped demo scene replayed through the reference frame by frame as
+    cb_display does (CCDDemo/mainTorusknot.cpp:207-325): both objects the
+    shipped bunny (69,664 triangles), key frames from the two shipped .ani
+    files, every one of the 303 frames seeded with the models' last_tri that
+    the previous frame left.  Stores each frame's seeds, results and contacts,
+    and the bunny exactly: its vertices are six-decimal text, kept as integer
+    millionths (integer / 1e6 is the correctly rounded double that the
+    reader's %lf gives)."""
+    path = os.path.join(REF_DIR, "tri_models", "bunny_noholes.tri")
+    bunny = meshes.read_tri(path)
+    tok = open(path).read().split()
+    nv = int(tok[1])
+    micro = np.array([int(t.replace(".", "")) for t in tok[3:3 + 3 * nv]], dtype=np.int64).reshape(nv, 3)
+    assert np.abs(micro).max() < 2 ** 31 and all(len(t.split(".")[1]) == 6 for t in tok[3:3 + 3 * nv])
+    assert np.array_equal(micro / 1e6, bunny.verts)
+    a0 = replay.read_ani(os.path.join(REF_DIR, "models", "torusknot1.ani"))
+    a1 = replay.read_ani(os.path.join(REF_DIR, "models", "torusknot2.ani"))
+    n = len(a0[0])
+    qint, poses = replay.demo_queries(a0, a1)
+    params = replay.demo_params()
+    res = np.zeros(n, dtype=RESULT_DTYPE)
+    cons, offs = [], [0]
+    with quiet_stdout():
+        ha, hb = ref.model(bunny), ref.model(bunny)
+        for i in range(n):
+            qint[i, 2], qint[i, 3] = ref.last_tri(ha), ref.last_tri(hb)
+            r, c = ref.solve(ha, hb, poses[i], int(qint[i, 2]), int(qint[i, 3]), params, shipped=True)
+            res[i] = r
+            cons.append(np.ascontiguousarray(c[::-1]))  # push_front list: stored in visiting order
+            offs.append(offs[-1] + len(c))
+    np.savez_compressed(os.path.join(HERE, "demo_scene_ref.npz"), verts_micro=micro.astype(np.int32),
+                        faces=bunny.faces.astype(np.int32), qint=qint, poses=poses, results=res,
+                        contacts=np.concatenate(cons) if cons else np.zeros(0, CONTACT_DTYPE),
+                        contact_offsets=np.array(offs))
+    print(f"demo_scene_ref.npz: {n} frames, {int((1 - res['collisionfree']).sum())} colliding, "
+          f"{offs[-1]} contacts, mean numCA {res['numCA'].mean():.2f}")
+
+
 def main():
     build(ref=True)
     ref = Ref()
+    if sys.argv[1:] == ["demo"]:
+        demo_scene_fixture(ref)
+        return
     if sys.argv[1:] == ["static"]:
         static_query_fixtures(ref)
         return
@@ -346,6 +392,7 @@ def main():
     canonical_fixtures(ref)
     distance_fixtures(ref)
     static_query_fixtures(ref)
+    demo_scene_fixture(ref)
 
 
 if __name__ == "__main__":

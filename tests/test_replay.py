@@ -30,7 +30,9 @@ def test_demo_frame_steps_and_queries():
     assert replay.demo_steps(101) == (101, 102, 101) and replay.demo_steps(202) == (202, 203, 202)
     a0, a1 = replay.synthetic_scene(12)
     qint, poses = replay.demo_queries(a0, a1, seeds=(3, 5))
-    assert qint.shape == (11, 4) and (qint[:, 2] == 3).all() and (qint[:, 3] == 5).all()
+    assert qint.shape == (12, 4) and (qint[:, 2] == 3).all() and (qint[:, 3] == 5).all()
+    per = np.arange(24, dtype=np.int32).reshape(12, 2)
+    assert np.array_equal(replay.demo_queries(a0, a1, seeds=per)[0][:, 2:4], per)
     i = 7
     assert np.array_equal(poses[i, 0:9], a0[0][0].reshape(9)) and np.array_equal(poses[i, 12:21], a0[0][1].reshape(9))
     assert np.array_equal(poses[i, 24:33], a1[0][i].reshape(9)) and np.array_equal(poses[i, 36:45], a1[0][i].reshape(9))
@@ -62,3 +64,56 @@ def test_gpu_demo_replay_matches_port(gpu_ctx, port):
     for i in range(len(q)):
         n = min(int(pres[i]["num_contact"]), 256)
         assert bits(con[i]["tri_a"]) == bits(pcon[i][:n]["tri_a"]) and bits(con[i]["pa"]) == bits(pcon[i][:n]["pa"])
+
+
+def _demo_scene():
+    from c2a_testutil import GOLDEN
+
+    z = np.load(f"{GOLDEN}/demo_scene_ref.npz")
+    bunny = meshes.Mesh("bunny_noholes", z["verts_micro"] / 1e6, z["faces"], np.zeros((1, 3)), 0.0)
+    return bunny, z
+
+
+def _check_demo(res, con, z):
+    """Every field and contact bit for bit; mint on collision-free frames only:
+    the shipped C2A_Solve leaves the contact query's reset value 1 there
+    (C2A.cpp:1757)."""
+    from c2a_testutil import RESULT_FIELDS as F, result_mismatches
+
+    exp = z["results"]
+    bad = result_mismatches(res, exp, con, z["contacts"], z["contact_offsets"], fields=[f for f in F if f != "mint"])
+    assert not bad, bad[:10]
+    free = exp["collisionfree"] == 1
+    assert bits(res["mint"][free]) == bits(exp["mint"][free]) and (exp["mint"][~free] == 1.0).all()
+
+
+def test_shipped_demo_scene_on_the_oracle(port):
+    """The shipped scene (bunny against bunny, torusknot1/2.ani, 303 frames) on
+    the oracle port against the reference's own per-frame results and
+    contacts, with the seeds the demo's last_tri chain gave each frame."""
+    bunny, z = _demo_scene()
+    assert bunny.num_tris == 69664
+    assert z["poses"].shape == (303, 48) and z["qint"].shape == (303, 4)
+    res, con = port.solve_batch(port.models([bunny, bunny]), z["qint"], z["poses"], replay.demo_params(), threads=8,
+                                contacts_per_query=128)
+    _check_demo(res, con, z)
+    assert (z["results"]["collisionfree"] == 0).sum() > 100
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", ["auto", "thread", "spec"])
+def test_gpu_shipped_demo_scene_matches_reference(gpu_ctx, engine):
+    """Every frame of the shipped scene on the GPU through c2a_solve_batch:
+    every result field and every contact bit for bit as the reference
+    computed them."""
+    from c2a_gb300 import api
+
+    bunny, z = _demo_scene()
+    ids = gpu_ctx.models([bunny, bunny])
+    q = z["qint"].copy()
+    q[:, 0], q[:, 1] = ids
+    prm = dict(replay.demo_params(), engine={"auto": api.ENGINE_AUTO, "thread": api.ENGINE_THREAD,
+                                             "spec": api.ENGINE_SPEC}[engine])
+    res, con = gpu_ctx.solve(q, z["poses"], prm, contacts_per_query=128)
+    _check_demo(res, [con[i] for i in range(len(q))], z)
+    assert (res["status"] == 0).all()
