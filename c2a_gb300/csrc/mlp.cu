@@ -408,6 +408,93 @@ c2a_status c2a_mlp_expect(const float *logits, int32_t M, int32_t N, float *out,
     return launch_status();
 }
 
+namespace {
+constexpr int kOrderChunk = 1024; /* keys per block of the ordering kernels */
+
+__device__ __forceinline__ int order_bin(float key, float key_max)
+{
+    float t = key_max > 0.f ? __fdiv_rn(key, key_max) : 0.f;
+    t = t < 0.f ? 0.f : (t > 1.f ? 1.f : t);
+    if (t != t) t = 0.f; /* NaN: last */
+    int level = (int)__fadd_rn(__fmul_rn(t, (float)(C2A_ORDER_BINS - 1)), 0.5f); /* no contraction */
+    return (C2A_ORDER_BINS - 1) - level; /* bin 0 holds the largest keys */
+}
+
+/* per-chunk histograms, bin-major: hist[bin * chunks + chunk] */
+__global__ void __launch_bounds__(kOrderChunk) k_order_hist(const float *__restrict__ key, int n, float key_max,
+                                                            int32_t *__restrict__ hist, int chunks)
+{
+    __shared__ int32_t h[C2A_ORDER_BINS];
+    for (int b = threadIdx.x; b < C2A_ORDER_BINS; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * kOrderChunk + threadIdx.x;
+    if (i < n) atomicAdd(&h[order_bin(key[i], key_max)], 1);
+    __syncthreads();
+    for (int b = threadIdx.x; b < C2A_ORDER_BINS; b += blockDim.x) hist[(size_t)b * chunks + blockIdx.x] = h[b];
+}
+
+/* exclusive scan of the bin-major histogram in place (one block) */
+__global__ void __launch_bounds__(kOrderChunk) k_order_scan(int32_t *__restrict__ hist, int total)
+{
+    __shared__ int32_t part[kOrderChunk];
+    const int per = (total + kOrderChunk - 1) / kOrderChunk;
+    const int lo = threadIdx.x * per, hi = min(lo + per, total);
+    int32_t s = 0;
+    for (int k = lo; k < hi; k++) s += hist[k];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < kOrderChunk; off <<= 1) { /* inclusive Hillis-Steele scan of the partial sums */
+        const int32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
+    for (int k = lo; k < hi; k++) {
+        const int32_t c = hist[k];
+        hist[k] = run;
+        run += c;
+    }
+}
+
+/* scatter: a key's place is its (bin, chunk) offset plus the number of keys
+ * of the same bin before it in its chunk (warps in order, lanes by match) */
+__global__ void __launch_bounds__(kOrderChunk) k_order_scatter(const float *__restrict__ key, int n, float key_max,
+                                                               const int32_t *__restrict__ offs, int chunks,
+                                                               int32_t *__restrict__ order)
+{
+    __shared__ int32_t seen[C2A_ORDER_BINS];
+    for (int b = threadIdx.x; b < C2A_ORDER_BINS; b += blockDim.x) seen[b] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * kOrderChunk + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int bin = i < n ? order_bin(key[i], key_max) : -1 - lane; /* out-of-range lanes match nobody */
+    const unsigned same = __match_any_sync(0xffffffffu, bin);
+    const int before = __popc(same & ((1u << lane) - 1u));
+    for (int w = 0; w < kOrderChunk / 32; w++) {
+        if (warp == w && i < n) {
+            order[offs[(size_t)bin * chunks + blockIdx.x] + seen[bin] + before] = i;
+        }
+        __syncthreads();
+        if (warp == w && i < n && before == 0) seen[bin] += __popc(same);
+        __syncthreads();
+    }
+}
+} // namespace
+
+c2a_status c2a_mlp_order_desc(const float *key, int32_t n, float key_max, int32_t *order, int32_t *scratch,
+                              void *stream)
+{
+    if (n < 0 || (n > 0 && (!key || !order || !scratch))) return C2A_ERR_INVALID_ARGUMENT;
+    if (n == 0) return C2A_OK;
+    const int chunks = (n + kOrderChunk - 1) / kOrderChunk;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_order_hist<<<chunks, kOrderChunk, 0, s>>>(key, n, key_max, scratch, chunks);
+    k_order_scan<<<1, kOrderChunk, 0, s>>>(scratch, chunks * C2A_ORDER_BINS);
+    k_order_scatter<<<chunks, kOrderChunk, 0, s>>>(key, n, key_max, scratch, chunks, order);
+    return launch_status();
+}
+
 c2a_status c2a_mlp_colsum(const uint16_t *in, int32_t M, int32_t N, float *out, void *stream)
 {
     if (!in || !out || M <= 0 || N <= 0) return C2A_ERR_INVALID_ARGUMENT;

@@ -42,8 +42,14 @@ TOPK = 8
 ROW_ALIGN = 128
 
 MLP_SYMBOLS = ["c2a_mlp_adam", "c2a_mlp_assemble", "c2a_mlp_colsum", "c2a_mlp_embed_backward", "c2a_mlp_expect",
-               "c2a_mlp_gelu_backward", "c2a_mlp_gemm", "c2a_mlp_softmax_xent", "c2a_mlp_topk",
-               "c2a_mlp_transpose"]
+               "c2a_mlp_gelu_backward", "c2a_mlp_gemm", "c2a_mlp_order_desc", "c2a_mlp_softmax_xent",
+               "c2a_mlp_topk", "c2a_mlp_transpose"]
+ORDER_BINS = 1024  # C2A_ORDER_BINS
+
+
+def order_scratch(n: int) -> int:
+    """int32 scratch of c2a_mlp_order_desc (C2A_ORDER_SCRATCH)."""
+    return (n + 1023) // 1024 * ORDER_BINS
 
 BIAS, GELU = 1, 2
 
@@ -62,6 +68,7 @@ def bind(lib=None):
         "c2a_mlp_embed_backward": [vp, vp, vp, i32, i32, vp, vp],
         "c2a_mlp_topk": [vp, i32, i32, i32, vp, vp],
         "c2a_mlp_expect": [vp, i32, i32, vp, vp],
+        "c2a_mlp_order_desc": [vp, i32, f32, vp, vp, vp],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -518,7 +525,15 @@ class CostOrder:
         return out[:n]
 
     def order(self, feat_dev, ia_dev, ib_dev):
-        """The schedule: query indices by decreasing expected cost (device int32)."""
+        """The schedule: query indices by decreasing expected cost (device int32),
+        the library's stable counting sort over the expected bucket quantised to
+        1/16 of a bucket (c2a_mlp_order_desc)."""
         torch = self.net.torch
         e = self.expected(feat_dev, ia_dev, ib_dev)
-        return torch.argsort(e, descending=True, stable=True).to(torch.int32)
+        n = e.shape[0]
+        if getattr(self, "_scratch", None) is None or self._scratch.numel() < order_scratch(n):
+            self._scratch = torch.empty(order_scratch(n), dtype=torch.int32, device=self.net.dev)
+        out = torch.empty(n, dtype=torch.int32, device=self.net.dev)
+        _ok(self.net.lib.c2a_mlp_order_desc(_p(e), n, float(COST_BUCKETS - 1), _p(out), _p(self._scratch),
+                                            self.net._s()), "c2a_mlp_order_desc")
+        return out

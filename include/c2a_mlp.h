@@ -81,6 +81,16 @@ c2a_status c2a_mlp_embed_backward(const float *dx, const int32_t *ia, const int3
 /* the k (<= 16) largest of N logits per row, in decreasing order (ties: lower index first) */
 c2a_status c2a_mlp_topk(const float *logits, int32_t M, int32_t N, int32_t k, int32_t *index, void *stream);
 
+/* The schedule from expected costs: order[0..n) = the indices 0..n-1 by
+ * decreasing key, key in [0, key_max] quantised to C2A_ORDER_BINS levels,
+ * ties (same level) in increasing index (a stable, deterministic counting
+ * sort: histogram per 1024-key chunk, one scan, a ranked scatter).  scratch:
+ * C2A_ORDER_SCRATCH(n) int32 of device memory. */
+#define C2A_ORDER_BINS 1024
+#define C2A_ORDER_SCRATCH(n) ((int64_t)(((n) + 1023) / 1024) * C2A_ORDER_BINS)
+c2a_status c2a_mlp_order_desc(const float *key, int32_t n, float key_max, int32_t *order, int32_t *scratch,
+                              void *stream);
+
 #ifdef __cplusplus
 }
 #endif

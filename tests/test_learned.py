@@ -282,3 +282,29 @@ def test_gpu_cost_order_learns(gpu_ctx):
     assert r > 0.8, r  # held-out rank correlation of predicted and true cost
     o = model.order(dev(feat), dev(z), dev(z)).cpu().numpy()
     assert sorted(o.tolist()) == list(range(n))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 1000, 70001])
+def test_gpu_order_desc_is_a_stable_counting_sort(gpu_ctx, n):
+    """c2a_mlp_order_desc against numpy: indices by decreasing quantised key,
+    ties in increasing index; keys outside [0, key_max] and NaN clamp."""
+    import torch
+
+    rng = np.random.default_rng(64 + n)
+    key = (rng.integers(0, 40, n) * 1.5 + rng.normal(scale=1e-4, size=n)).astype(np.float32)
+    key[:: 97] = -3.0
+    key[5:: 101] = 1e9
+    if n > 7:
+        key[7] = np.nan
+    key_max = np.float32(63.0)
+    t = np.clip(np.where(np.isnan(key), 0, key) / key_max, 0, 1).astype(np.float32)
+    level = (t * np.float32(learned.ORDER_BINS - 1) + np.float32(0.5)).astype(np.int32)
+    expect = np.argsort(-level, kind="stable")
+    lib = learned.bind()
+    d_k = torch.tensor(key, device="cuda")
+    d_o = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    scratch = torch.empty(learned.order_scratch(n), dtype=torch.int32, device="cuda")
+    assert lib.c2a_mlp_order_desc(d_k.data_ptr(), n, 63.0, d_o.data_ptr(), scratch.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(d_o.cpu().numpy(), expect)

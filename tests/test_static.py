@@ -114,7 +114,7 @@ def test_tolerance_matches_oracle_on_large_meshes(gpu_ctx, port):
     rng = np.random.default_rng(73)
     n = 384
     ab = rng.integers(0, 3, (n, 2))
-    R, T = _placements(n, 74)
+    R, T = _placements(n, 74, reach=3.0)
     tol = rng.uniform(0.0, 0.2, n)
     tol[::17] = 0.0
     q = np.zeros((n, 4), dtype=np.int32)
