@@ -141,7 +141,7 @@ def test_collide_matches_oracle_on_large_meshes(gpu_ctx, port, flag):
     rng = np.random.default_rng(75 + flag)
     n = 256
     ab = rng.integers(0, 3, (n, 2))
-    R, T = _placements(n, 77 + flag, reach=1.5)
+    R, T = _placements(n, 77 + flag, reach=3.0)
     q = np.zeros((n, 4), dtype=np.int32)
     q[:, 0] = [mids[a] for a in ab[:, 0]]
     q[:, 1] = [mids[b] for b in ab[:, 1]]
