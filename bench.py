@@ -207,7 +207,7 @@ def config_dict(wl, args, queries=None):
             "contacts_per_query": CONTACT_SLOTS, "parallelism": f"replicas x{args.gpus}"}
 
 
-def implementation_dict(args):
+def implementation_dict(args, engine=None):
     if args.impl == "reference":
         return {"what": "the CPU oracle port of the reference (bit-identical to the reference compiled here), "
                         "one query per task, all host threads"}
@@ -218,7 +218,8 @@ def implementation_dict(args):
                          "node-pair test split across the lanes",
                  "thread": "reference order, one thread per query"}
     return {"engine": args.engine, "order": args.order if args.mode == "reference" else "geometric",
-            "traversal": traversal.get(ENGINE_OF.get(args.engine, args.engine), "canonical front")
+            "launch": "CUDA graph replay of the solve's launches (tune.GraphSolve)",
+            "traversal": traversal.get(engine or ENGINE_OF.get(args.engine, args.engine), "canonical front")
             if args.mode == "reference" else
             "canonical: each step seeded with the exact closest pair (the reference's C2A_Distance), order-free "
             "front traversal; bit-identical to that composition of the reference's functions",
@@ -299,9 +300,22 @@ def main():
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.Stream()
 
+    from c2a_gb300 import tune
+
+    tuned = None
+    if args.engine == "auto":  # the autotuner's launch for this kind of batch (never changes a result)
+        t_tune = time.time()
+        tuned = tune.Tuner(ctx, sample=4096, repeats=1).choose(d_q, n, wl.params, CONTACT_SLOTS, stream=stream)
+        wl.params.update(engine=tuned["params"]["engine"], warps_per_sm=tuned["params"]["warps_per_sm"])
+        tuned = {"choice": tuned["record"]["choice"]["name"], "sample_ms": tuned["record"]["ms"],
+                 "sample_queries": tuned["record"]["sample_queries"], "cached": tuned["record"]["cached"],
+                 "tune_s": time.time() - t_tune}
+    run_engine = tuned["choice"].split("/")[0] if tuned else args.engine
+    # every timed step replays a CUDA graph of the solve's launches on fixed buffers
+    plain_graph = tune.GraphSolve(ctx, d_q, n, wl.params, d_r, d_c, CONTACT_SLOTS, stream=stream)
+
     def plain_step():
-        ctx.solve_device(d_q.data_ptr(), n, wl.params, d_r.data_ptr(), d_c.data_ptr(), CONTACT_SLOTS,
-                         stream=stream.cuda_stream)
+        plain_graph.replay()
 
     learned_info = None
     step = plain_step
@@ -330,11 +344,14 @@ def main():
                         "epochs": epochs, "final_loss": hist[-1], "held_out_rank_correlation": rank_r,
                         "used": rank_r >= 0.6, "setup_s": time.time() - t_setup}
 
+        d_order = torch.arange(n, dtype=torch.int32, device="cuda")
+        ordered_graph = tune.GraphSolve(ctx, d_q, n, wl.params, d_r, d_c, CONTACT_SLOTS, d_order=d_order,
+                                        stream=stream)
+
         def learned_step():
             with torch.cuda.stream(stream):
-                order = cost_model.order(feat_dev, zeros_dev, zeros_dev)
-                ctx.solve_ordered(d_q.data_ptr(), n, wl.params, order.data_ptr(), d_r.data_ptr(), d_c.data_ptr(),
-                                  CONTACT_SLOTS, stream=stream.cuda_stream)
+                d_order.copy_(cost_model.order(feat_dev, zeros_dev, zeros_dev))
+            ordered_graph.replay()
 
         if learned_info["used"]:  # a model that does not rank held-out costs leaves the geometric order
             step = learned_step
@@ -361,10 +378,16 @@ def main():
     clk = clocks.stop()
     if dist:
         dist.barrier()
+    # graph replays do not pass through the library's launch counter: count their kernels per replay
     launches = ctx.launches() - launches0
+    if step is plain_step:
+        launches += plain_graph.kernels * args.steps
+    else:
+        launches += ordered_graph.kernels * args.steps
     if learned_info is not None:  # the geometric order on the same batch, for the comparison
         if learned_info["used"]:
-            launches += 6 * args.steps  # the network per step: assembly, four GEMMs, expected bucket
+            # the network and the schedule per step: assembly, four GEMMs, expected bucket, three ordering kernels
+            launches += 9 * args.steps
         res_learned = d_r.cpu().numpy().copy()
         plain_step()
         stream.synchronize()
@@ -410,7 +433,7 @@ def main():
                 "frac": achieved / (fma_peak / 1e9), "traffic": None,
                 "peak_source": "measured in this run: c2a_probe_fp64_peak (FP64 FMA chains on every SM, best of 5)",
                 "peak_unfused": add_peak / 1e9, "frac_of_unfused": achieved / (add_peak / 1e9),
-                "kernel": KERNELS.get((args.mode, args.engine)),
+                "kernel": KERNELS.get((args.mode, run_engine)),
                 "flops_per_bv_test": F_BV, "flops_per_tri_test": F_TRI, "algorithmic_flops_per_launch": alg_flops,
                 "num_bv_tests": bv, "num_tri_tests": tri,
                 "hbm": {"achieved": alg_bytes / launch_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
@@ -486,9 +509,10 @@ def main():
                 "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
-                "config": config_dict(wl, args), "implementation": implementation_dict(args), "clocks": clk, "gpu_launches": launches, "e2e": e2e,
+                "config": config_dict(wl, args), "implementation": implementation_dict(args, run_engine), "clocks": clk,
+                "gpu_launches": launches, "e2e": e2e,
                 "roofline": roofline, "cpu_baseline": cpu,
-                "learned_order": learned_info,
+                "learned_order": learned_info, "tuned_launch": tuned,
                 "collision_fraction": float(1 - res["collisionfree"].mean()),
                 "mean_numCA": float(res["numCA"].mean()), "step_ms": step_ms}
         print(json.dumps(line), flush=True)

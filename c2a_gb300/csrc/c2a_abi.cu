@@ -178,7 +178,7 @@ c2a_status ensure_fronts(c2a_context *ctx, size_t warps, size_t want)
 
 bool params_ok(const c2a_params *p)
 {
-    return p && p->max_iters >= 0 && p->contacts_per_query >= 0 &&
+    return p && p->max_iters >= 0 && p->contacts_per_query >= 0 && p->warps_per_sm >= 0 && p->reserved == 0 &&
            (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL) && p->engine >= C2A_ENGINE_AUTO &&
            p->engine <= C2A_ENGINE_SPEC && !(p->mode == C2A_MODE_REFERENCE && p->engine == C2A_ENGINE_BATCHED) &&
            !(p->mode == C2A_MODE_CANONICAL && (p->engine == C2A_ENGINE_THREAD || p->engine == C2A_ENGINE_SPEC));
@@ -201,11 +201,19 @@ c2a_status check_depths(c2a_context *ctx, int *deepest_out = nullptr)
 struct Shape {
     int blocks, threads;
 };
-Shape shape_for(c2a_context *ctx, int n)
+/* resident blocks per SM: what fits (occ), capped by the caller's warps per SM */
+int blocks_per_sm(int occ, int warps_per_sm, int threads)
+{
+    if (warps_per_sm <= 0) return occ;
+    const int want = warps_per_sm / (threads / 32);
+    return want < 1 ? 1 : (want < occ ? want : occ);
+}
+
+Shape shape_for(c2a_context *ctx, int n, int warps_per_sm)
 {
     int threads = kThreads;
     if ((n + kThreads - 1) / kThreads < 2 * ctx->sm_count) threads = 32;
-    const int most = ctx->sm_count * 8 * (kThreads / threads);
+    const int most = ctx->sm_count * blocks_per_sm(8 * (kThreads / threads), warps_per_sm, threads);
     int need = (n + threads - 1) / threads;
     if (need < 1) need = 1;
     return Shape{need < most ? need : most, threads};
@@ -577,7 +585,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
             C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_canonical_kernel, kThreads, 0));
             ctx->canonical_blocks_per_sm = occ > 0 ? occ : 1;
         }
-        const int most = ctx->sm_count * ctx->canonical_blocks_per_sm;
+        const int most = ctx->sm_count * blocks_per_sm(ctx->canonical_blocks_per_sm, prm.warps_per_sm, kThreads);
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
         const int blocks = need < most ? need : most;
         st = ensure_fronts(ctx, (size_t)blocks * (kThreads / 32), (size_t)most * (kThreads / 32));
@@ -620,7 +628,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
             ctx->spec_cap = cap;
             ctx->spec_nrec = nrec;
         }
-        const int most = ctx->sm_count * ctx->spec_blocks_per_sm;
+        const int most = ctx->sm_count * blocks_per_sm(ctx->spec_blocks_per_sm, prm.warps_per_sm, kThreads);
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
         const int blocks = need < most ? need : most;
         const size_t gbytes = spec_global_bytes(nrec) * (size_t)blocks * (kThreads / 32);
@@ -663,7 +671,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
             ctx->warp_blocks_per_sm = occ > 0 ? occ : 1;
             ctx->warp_cap = cap;
         }
-        const int most = ctx->sm_count * ctx->warp_blocks_per_sm;
+        const int most = ctx->sm_count * blocks_per_sm(ctx->warp_blocks_per_sm, prm.warps_per_sm, kThreads);
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);
         if (!user_order) { /* queries whose bounding spheres approach go first */
             C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 1, 0, 2 * sizeof(unsigned int), s));
@@ -679,7 +687,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
         C2A_CUDA(cudaGetLastError());
         return C2A_OK;
     }
-    const Shape sh = shape_for(ctx, n);
+    const Shape sh = shape_for(ctx, n, prm.warps_per_sm);
     c2a_solve_kernel<<<sh.blocks, sh.threads, 0, s>>>(d_queries, n, ctx->d_models, (int)ctx->models.size(), prm,
                                                        d_results, d_contacts, ctx->d_counter);
     ctx->launches++;
@@ -841,7 +849,7 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
     C2A_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned int), s)); /* the last call left its count here */
     c2a_params prm = *params;
     if (!d_contacts) prm.contacts_per_query = 0;
-    const Shape sh = shape_for(ctx, n);
+    const Shape sh = shape_for(ctx, n, prm.warps_per_sm);
     c2a_solve_kernel<<<sh.blocks, sh.threads, 0, s>>>(d_queries, n, d_table, (int)num_models, prm, d_results,
                                                        d_contacts, d_counter);
     ctx->launches++;

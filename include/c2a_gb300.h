@@ -81,6 +81,9 @@ typedef struct c2a_params {
     int32_t contacts_per_query; /* contact slots per query in the output buffer */
     int32_t mode;               /* C2A_MODE_REFERENCE or C2A_MODE_CANONICAL */
     int32_t engine;             /* C2A_ENGINE_*; never changes a result */
+    int32_t warps_per_sm;       /* launch shape: resident warps per SM of the solve kernel, 0 the most
+                                   that fit (c2a_gb300.tune picks it); never changes a result */
+    int32_t reserved;           /* 0 */
 } c2a_params;
 
 /* C2A_MODE_REFERENCE: the reference's results bit for bit (its depth-first

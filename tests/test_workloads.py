@@ -81,10 +81,16 @@ def test_near_contact_placement_with_port(port):
     assert (np.abs(np.sum(v * nrm, axis=1)) <= np.sin(np.deg2rad(5.0)) + 1e-9).all()
 
 
+_GPU_IDS = {}
+
+
 def gpu_vs_port(ctx, port, wl, mode=0, engine=0):
     from c2a_gb300 import api
 
-    ids = np.array([ctx.model(m) for m in wl.meshes])
+    key = (id(ctx), id(wl))
+    if key not in _GPU_IDS:  # each workload's models built once per context
+        _GPU_IDS[key] = np.array([ctx.model(m) for m in wl.meshes])
+    ids = _GPU_IDS[key]
     q = wl.qint.copy()
     q[:, 0] = ids[wl.qint[:, 0]]
     q[:, 1] = ids[wl.qint[:, 1]]
@@ -106,6 +112,35 @@ def gpu_vs_port(ctx, port, wl, mode=0, engine=0):
 @pytest.mark.parametrize("mode,engine", [(0, 1), (0, 3), (1, 1), (1, 2)])
 def test_gpu_config3_matches_port(gpu_ctx, port, mode, engine):
     gpu_vs_port(gpu_ctx, port, small_config3(n=128, seed=33), mode, engine)
+
+
+@pytest.fixture(scope="module")
+def config3_full():
+    """Config 3 as specified: 4,096 pairs from a pool of 12 meshes, 1k-200k triangles log-uniform."""
+    return workloads.config3(n=4096, seed=3, device="cpu")
+
+
+@pytest.fixture(scope="module")
+def config3_top():
+    """The top of config 3's range: six meshes of 100k-200k triangles (knots and
+    clustered soups; icospheres stop at 81,920), 2,048 pairs."""
+    return workloads.config3(n=2048, seed=21, pool=6, tri_range=(100000, 200000), device="cpu")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", ["full", "top"])
+@pytest.mark.parametrize("mode,engine", [(0, 1), (0, 3), (0, 4), (1, 1), (1, 2)])
+def test_gpu_config3_full_size_matches_port(gpu_ctx, port, request, which, mode, engine):
+    """Every query of the full-size uneven batches, REFERENCE (warp, thread,
+    speculative engines) and CANONICAL (warp, batched), bit for bit against
+    the oracle; no query may overflow a stack or be rejected."""
+    wl = request.getfixturevalue(f"config3_{which}")
+    tris = sorted(m.num_tris for m in wl.meshes)
+    if which == "top":
+        assert tris[-1] >= 190000 and sum(t >= 150000 for t in tris) >= 2
+    else:
+        assert tris[0] < 2000 and len(tris) == 12
+    gpu_vs_port(gpu_ctx, port, wl, mode, engine)
 
 
 @pytest.mark.gpu
