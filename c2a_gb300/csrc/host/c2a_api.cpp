@@ -491,3 +491,104 @@ C2A_Result C2A_Solve(Transform *trans00, Transform *trans01, C2A_Model *obj1, Tr
     number_of_iteration = dres.numCA;
     return TOCFound;
 }
+
+/* ----------------------------------------------- static proximity queries */
+namespace {
+/* model a placed by (R1, T1), model b by (R2, T2); seeds from the models' last_tri */
+c2a_query static_query(const PQP_REAL R1[3][3], const PQP_REAL T1[3], const C2A_Model *o1, const PQP_REAL R2[3][3],
+                       const PQP_REAL T2[3], const C2A_Model *o2)
+{
+    c2a_query q;
+    std::memset(&q, 0, sizeof(q));
+    q.model_a = o1 ? o1->model_id : -1;
+    q.model_b = o2 ? o2->model_id : -1;
+    q.seed_a = tri_index(o1, o1 ? o1->last_tri : nullptr, 0);
+    q.seed_b = tri_index(o2, o2 ? o2->last_tri : nullptr, 0);
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 3; j++) {
+            q.pose[3 * i + j] = R1[i][j];
+            q.pose[24 + 3 * i + j] = R2[i][j];
+        }
+        q.pose[9 + i] = T1[i];
+        q.pose[33 + i] = T2[i];
+    }
+    return q;
+}
+
+/* the result's R, T: model 2 in model 1's frame (MTxM, VmV, MTxV) */
+void relative(const PQP_REAL R1[3][3], const PQP_REAL T1[3], const PQP_REAL R2[3][3], const PQP_REAL T2[3],
+              PQP_REAL R[3][3], PQP_REAL T[3])
+{
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) R[i][j] = R1[0][i] * R2[0][j] + R1[1][i] * R2[1][j] + R1[2][i] * R2[2][j];
+    const PQP_REAL d[3] = {T2[0] - T1[0], T2[1] - T1[1], T2[2] - T1[2]};
+    for (int i = 0; i < 3; i++) T[i] = R1[0][i] * d[0] + R1[1][i] * d[1] + R1[2][i] * d[2];
+}
+} // namespace
+
+int C2A_Distance(C2A_DistanceResult *result, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                 PQP_REAL T2[3], C2A_Model *o2, PQP_REAL rel_err, PQP_REAL abs_err, int qsize)
+{
+    if (!result || !o1 || !o2 || rel_err != 0 || abs_err != 0) return C2A_ERR_INVALID_ARGUMENT;
+    const c2a_query q = static_query(R1, T1, o1, R2, T2, o2);
+    c2a_distance_result r;
+    const c2a_status st = c2a_distance_batch(o1->ctx, &q, 1, &r);
+    if (st) return st;
+    relative(R1, T1, R2, T2, result->R, result->T);
+    result->rel_err = rel_err;
+    result->abs_err = abs_err;
+    result->qsize = qsize;
+    result->distance = r.distance;
+    std::memcpy(result->p1, r.p1, sizeof(result->p1));
+    std::memcpy(result->p2, r.p2, sizeof(result->p2));
+    result->last_triA = o1->GetTriangle(r.tri_a);
+    result->last_triB = o2->GetTriangle(r.tri_b);
+    result->t1 = result->last_triA->id;
+    result->t2 = result->last_triB->id;
+    result->num_bv_tests = result->num_tri_tests = 0; /* the batch query reports no counters */
+    return C2A_OK;
+}
+
+int C2A_Tolerance(PQP_ToleranceResult *res, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                  PQP_REAL T2[3], C2A_Model *o2, PQP_REAL tolerance, int qsize)
+{
+    (void)qsize; /* the qsize-2 order (the reference's default and the demo's) */
+    if (!res || !o1 || !o2) return C2A_ERR_INVALID_ARGUMENT;
+    const c2a_query q = static_query(R1, T1, o1, R2, T2, o2);
+    c2a_tolerance_result r;
+    const double tol = tolerance;
+    const c2a_status st = c2a_tolerance_batch(o1->ctx, &q, 1, &tol, &r);
+    if (st) return st;
+    relative(R1, T1, R2, T2, res->R, res->T);
+    res->tolerance = tolerance < 0 ? 0 : tolerance;
+    res->closer_than_tolerance = r.closer;
+    res->distance = r.closer ? r.distance : 0.0;
+    std::memcpy(res->p1, r.p1, sizeof(res->p1));
+    std::memcpy(res->p2, r.p2, sizeof(res->p2));
+    res->num_bv_tests = (int)r.num_bv_tests;
+    res->num_tri_tests = (int)r.num_tri_tests;
+    return C2A_OK;
+}
+
+int C2A_Collide(PQP_CollideResult *result, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                PQP_REAL T2[3], C2A_Model *o2, int flag)
+{
+    if (!result || !o1 || !o2) return C2A_ERR_INVALID_ARGUMENT;
+    const c2a_query q = static_query(R1, T1, o1, R2, T2, o2);
+    c2a_collide_result r;
+    int slots = 1024;
+    std::vector<int32_t> pairs;
+    for (;;) { /* a second launch with room for every pair when the first overflowed */
+        pairs.assign(2 * (size_t)slots, 0);
+        const c2a_status st = c2a_collide_batch(o1->ctx, &q, 1, flag, slots, &r, pairs.data());
+        if (st) return st;
+        if (r.num_pairs <= slots) break;
+        slots = r.num_pairs;
+    }
+    relative(R1, T1, R2, T2, result->R, result->T);
+    result->pairs.resize((size_t)r.num_pairs);
+    for (int k = 0; k < r.num_pairs; k++) result->pairs[(size_t)k] = CollisionPair{pairs[2 * k], pairs[2 * k + 1]};
+    result->num_bv_tests = (int)r.num_bv_tests;
+    result->num_tri_tests = (int)r.num_tri_tests;
+    return C2A_OK;
+}

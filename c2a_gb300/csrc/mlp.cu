@@ -164,6 +164,221 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm(const uint16_t *__restric
             }
 }
 
+/* --------------------------------------------------- GEMM on tcgen05 */
+
+/* The same product on the fifth-generation tensor cores: a 128 x 128 output
+ * tile per CTA of four warps, the FP32 accumulator in tensor memory (128
+ * columns), K in steps of 64 through two shared-memory stages in the
+ * canonical no-swizzle K-major layout (8-row x 16-byte core matrices: the two
+ * K-neighbours of a core matrix 128 bytes apart (LBO), the M/N-neighbours 1 KiB
+ * apart (SBO)), filled with 16-byte cp.async copies while the tensor core
+ * works on the other stage.  One thread issues four tcgen05.mma (M 128, N 128,
+ * K 16, bf16 x bf16 -> FP32) per stage and commits them to the stage's
+ * mbarrier; the epilogue reads the accumulator with tcgen05.ld (warp w: rows
+ * 32 w .. 32 w + 31, one row per thread) and applies bias and GELU as the
+ * mma.sync kernel does.  Every mbarrier wait is bounded: a wait that runs
+ * out sets *err and the CTA still releases its tensor memory. */
+constexpr int kTcM = 128, kTcN = 128, kTcK = 64, kTcThreads = 128;
+constexpr int kTcStageBytes = (kTcM + kTcN) * kTcK * 2; /* 32 KiB: A tile then B tile */
+constexpr int kTcSmem = 2 * kTcStageBytes + 1024;      /* two stages + barriers; 4 CTAs per SM at most */
+constexpr uint32_t kTcLBO = 128, kTcSBO = 1024; /* memory strides: K-neighbour, M/N-neighbour core matrices */
+#ifndef C2A_TC_SWAP
+#define C2A_TC_SWAP 0 /* 1: the descriptor's two offset fields exchanged */
+#endif
+constexpr uint32_t kTcDescL = C2A_TC_SWAP ? kTcSBO : kTcLBO, kTcDescS = C2A_TC_SWAP ? kTcLBO : kTcSBO;
+__device__ int g_tc_err; /* set when a bounded mbarrier wait of k_gemm_tc ran out */
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+/* shared-memory matrix descriptor: start, LBO, SBO (all >> 4), version 1, no swizzle */
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((kTcDescL >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((kTcDescS >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+/* instruction descriptor of kind::f16: FP32 accumulator, bf16 A and B, both K-major, N 128, M 128 */
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
+                              ((uint32_t)(kTcM >> 4) << 24);
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+/* true once the barrier's phase with this parity completed; false after two
+ * seconds (non-blocking tests with a growing back-off) */
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    const uint64_t t0 = global_ns();
+    for (unsigned back = 0;; back = back < 256 ? back + 32 : 256) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done) return true;
+        if (global_ns() - t0 > 2000000000ull) return false;
+        __nanosleep(back);
+    }
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "setp.ne.u32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+                 ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(accumulate));
+}
+
+/* one stage: rows of A and B (K-chunks of 16 bytes) into the core-matrix layout; chunks past K are zero */
+__device__ __forceinline__ void tc_load_stage(const uint16_t *A, const uint16_t *B, int K, int m0, int n0, int k0,
+                                              unsigned char *stage)
+{
+#pragma unroll 4
+    for (int c = threadIdx.x; c < (kTcM + kTcN) * (kTcK / 8); c += kTcThreads) {
+        const int row = c >> 3, kc = c & 7; /* row 0..255 (A then B), 16-byte chunk along K */
+        const bool isB = row >= kTcM;
+        const int r = isB ? row - kTcM : row;
+        unsigned char *dst = stage + (isB ? kTcM * kTcK * 2 : 0) + (r >> 3) * kTcSBO + kc * kTcLBO + (r & 7) * 16;
+        const int k = k0 + kc * 8;
+        if (k < K) {
+            const uint16_t *src = isB ? B + (size_t)(n0 + r) * K + k : A + (size_t)(m0 + r) * K + k;
+            cp_async16(dst, src);
+        } else {
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const uint16_t *__restrict__ A, const uint16_t *__restrict__ B,
+                                                        const float *__restrict__ bias, int M, int N, int K, int flags,
+                                                        float *__restrict__ out_f32, uint16_t *__restrict__ out_bf16,
+                                                        int *__restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char *stage0 = tc_smem, *stage1 = tc_smem + kTcStageBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(tc_smem + 2 * kTcStageBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem + 2 * kTcStageBytes + 64);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
+
+    if (threadIdx.x == 0) {
+        mbar_init(bar0, 1);
+        mbar_init(bar1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)kTcN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    const int steps = (K + kTcK - 1) / kTcK;
+    bool ok = true;
+    uint32_t phase[2] = {0u, 0u};
+    tc_load_stage(A, B, K, m0, n0, 0, stage0);
+    cp_async_commit();
+    for (int s = 0; s < steps; s++) {
+        unsigned char *cur = (s & 1) ? stage1 : stage0;
+        unsigned char *nxt = (s & 1) ? stage0 : stage1;
+        if (s + 1 < steps) {
+            if (s >= 1) { /* the MMAs of step s - 1 read the other stage: wait for them before refilling it */
+                const int o = (s - 1) & 1;
+                ok = mbar_wait(o ? bar1 : bar0, phase[o]) && ok;
+                phase[o] ^= 1u;
+            }
+            tc_load_stage(A, B, K, m0, n0, (s + 1) * kTcK, nxt);
+            cp_async_commit();
+            cp_async_wait1();
+        } else {
+            cp_async_wait0();
+        }
+        /* this thread's copies into the current stage are done: publish them to the tensor core's proxy */
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t a0 = smem_u32(cur), b0 = smem_u32(cur + kTcM * kTcK * 2);
+#pragma unroll
+            for (int kk = 0; kk < kTcK / 16; kk++) /* K 16 = two core matrices = 2 LBO further along K */
+                tc_mma(tmem, tc_desc(a0 + kk * 2 * kTcLBO), tc_desc(b0 + kk * 2 * kTcLBO), (s > 0 || kk > 0) ? 1u : 0u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             (s & 1) ? bar1 : bar0)
+                         : "memory");
+        }
+    }
+    /* the last commit covers every MMA issued before it */
+    {
+        const int o = (steps - 1) & 1;
+        ok = mbar_wait(o ? bar1 : bar0, phase[o]) && ok;
+        if (steps >= 2) { /* the other stage's last commit completed with it; keep the phases consistent */
+            const int p = (steps - 2) & 1;
+            if (p != o) ok = mbar_wait(p ? bar1 : bar0, phase[p]) && ok;
+        }
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    /* epilogue: warp w owns accumulator rows 32 w .. 32 w + 31 (TMEM lanes), 32 columns per load */
+    const int row = m0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcN; c0 += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                     "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                     "[%32];\n"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                       "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                       "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                       "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (row < M) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 2) {
+                const int col = n0 + c0 + j;
+                float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
+                if (flags & C2A_MLP_BIAS) {
+                    v0 += bias[col];
+                    v1 += bias[col + 1];
+                }
+                const size_t o = (size_t)row * N + col;
+                if (out_f32) *reinterpret_cast<float2 *>(out_f32 + o) = make_float2(v0, v1);
+                if (out_bf16) {
+                    if (flags & C2A_MLP_GELU) {
+                        v0 = gelu(v0);
+                        v1 = gelu(v1);
+                    }
+                    *reinterpret_cast<uint32_t *>(out_bf16 + o) = (uint32_t)f2bf(v0) | ((uint32_t)f2bf(v1) << 16);
+                }
+            }
+        }
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"((uint32_t)kTcN));
+    }
+}
+
 /* ------------------------------------------------------ elementwise/rows */
 
 __global__ void k_transpose(const uint16_t *__restrict__ in, int rows, int cols, uint16_t *__restrict__ out)
@@ -369,14 +584,45 @@ int grid_for(int64_t count, int threads)
 
 extern "C" {
 
+#ifndef C2A_MLP_TCGEN05
+#define C2A_MLP_TCGEN05 0 /* 1: c2a_mlp_gemm runs k_gemm_tc */
+#endif
+
 c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias, int32_t M, int32_t N, int32_t K,
                         int32_t flags, float *out_f32, uint16_t *out_bf16, void *stream)
 {
     if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % kBM || N % kBN || K % kBK || ((flags & C2A_MLP_BIAS) && !bias))
         return C2A_ERR_INVALID_ARGUMENT;
+    if (C2A_MLP_TCGEN05) {
+        static bool attr = false;
+        if (!attr) {
+            if (cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess)
+                return C2A_ERR_CUDA;
+            attr = true;
+        }
+        int *err = nullptr;
+        if (cudaGetSymbolAddress((void **)&err, g_tc_err) != cudaSuccess) return C2A_ERR_CUDA;
+        const dim3 grid(N / kTcN, M / kTcM);
+        k_gemm_tc<<<grid, kTcThreads, kTcSmem, (cudaStream_t)stream>>>(A, B, bias, M, N, K, flags, out_f32, out_bf16,
+                                                                       err);
+        return launch_status();
+    }
     const dim3 grid(N / kBN, M / kBM);
     k_gemm<<<grid, kGemmThreads, 0, (cudaStream_t)stream>>>(A, B, bias, M, N, K, flags, out_f32, out_bf16);
     return launch_status();
+}
+
+c2a_status c2a_mlp_check(void *stream)
+{
+    int v = 0;
+    const int zero = 0;
+    if (cudaMemcpyFromSymbolAsync(&v, g_tc_err, sizeof(int), 0, cudaMemcpyDeviceToHost, (cudaStream_t)stream) !=
+            cudaSuccess ||
+        cudaMemcpyToSymbolAsync(g_tc_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, (cudaStream_t)stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+        return C2A_ERR_CUDA;
+    return v ? C2A_ERR_CUDA : C2A_OK;
 }
 
 c2a_status c2a_mlp_transpose(const uint16_t *in, int32_t rows, int32_t cols, uint16_t *out, void *stream)

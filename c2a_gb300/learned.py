@@ -41,7 +41,8 @@ OUT = NCLUSTER * NCLUSTER
 TOPK = 8
 ROW_ALIGN = 128
 
-MLP_SYMBOLS = ["c2a_mlp_adam", "c2a_mlp_assemble", "c2a_mlp_colsum", "c2a_mlp_embed_backward", "c2a_mlp_expect",
+MLP_SYMBOLS = ["c2a_mlp_adam", "c2a_mlp_assemble", "c2a_mlp_check", "c2a_mlp_colsum", "c2a_mlp_embed_backward",
+               "c2a_mlp_expect",
                "c2a_mlp_gelu_backward", "c2a_mlp_gemm", "c2a_mlp_order_desc", "c2a_mlp_softmax_xent",
                "c2a_mlp_topk", "c2a_mlp_transpose"]
 ORDER_BINS = 1024  # C2A_ORDER_BINS
@@ -69,6 +70,7 @@ def bind(lib=None):
         "c2a_mlp_topk": [vp, i32, i32, i32, vp, vp],
         "c2a_mlp_expect": [vp, i32, i32, vp, vp],
         "c2a_mlp_order_desc": [vp, i32, f32, vp, vp, vp],
+        "c2a_mlp_check": [vp],
     }
     for name, args in sig.items():
         f = getattr(lib, name)

@@ -15,6 +15,11 @@
  *   C2A_QueryContactOnly    C2A/C2A.h:292-299         (C2A/src/C2A.cpp:1968-1983)
  *   C2A_Model               C2A/C2A_Internal.h:32-81  (C2A/src/C2A_PQP.cpp:61-438)
  *   CInterpMotion_Linear    C2A/InterpMotion.h:164-226
+ *   C2A_Distance            C2A/C2A.h:256-260         (C2A/src/C2A_PQP.cpp:971-1056; rel_err = abs_err = 0)
+ *   C2A_Tolerance           C2A/src/C2A_PQP.cpp:1762-1845 (not in the reference's header)
+ *   C2A_Collide             C2A/C2A.h:249-253         (C2A/src/C2A_PQP.cpp:910-968)
+ *   PQP_CollideResult, PQP_ToleranceResult, C2A_DistanceResult: the accessors
+ *                           of the PQP result classes those queries fill
  *   C2A_SolveBatch          new: many independent C2A_Solve queries in one launch
  *
  * Differences a caller can see: C2A_Solve reads th_ca (the reference ignores
@@ -246,6 +251,83 @@ PQP_REAL C2A_QueryContact(CInterpMotion *objmotion1, CInterpMotion *objmotion2, 
 
 PQP_REAL C2A_QueryContactOnly(C2A_TimeOfContactResult *res, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1,
                               PQP_REAL R2[3][3], PQP_REAL T2[3], C2A_Model *o2, double threshold);
+
+/* ------------------------------------------------- static proximity queries */
+const int C2A_ALL_CONTACTS = 1;  /* every contacting triangle pair */
+const int C2A_FIRST_CONTACT = 2; /* the first one found */
+
+struct CollisionPair {
+    int id1, id2; /* caller triangle ids */
+};
+
+/* PQP_CollideResult's public face: counters and the contacting pairs in the
+ * order the query found them */
+class PQP_CollideResult {
+  public:
+    int num_bv_tests = 0, num_tri_tests = 0;
+    double query_time_secs = 0;
+    PQP_REAL R[3][3] = {}, T[3] = {}; /* model 2 in model 1's frame */
+    std::vector<CollisionPair> pairs;
+    int NumBVTests() { return num_bv_tests; }
+    int NumTriTests() { return num_tri_tests; }
+    double QueryTimeSecs() { return query_time_secs; }
+    int Colliding() { return !pairs.empty(); }
+    int NumPairs() { return (int)pairs.size(); }
+    int Id1(int k) { return pairs[k].id1; }
+    int Id2(int k) { return pairs[k].id2; }
+    void FreePairsList() { pairs.clear(); }
+};
+
+/* PQP_ToleranceResult's public face */
+class PQP_ToleranceResult {
+  public:
+    int num_bv_tests = 0, num_tri_tests = 0;
+    double query_time_secs = 0;
+    PQP_REAL R[3][3] = {}, T[3] = {};
+    int closer_than_tolerance = 0;
+    PQP_REAL tolerance = 0, distance = 0, p1[3] = {}, p2[3] = {};
+    int NumBVTests() { return num_bv_tests; }
+    int NumTriTests() { return num_tri_tests; }
+    double QueryTimeSecs() { return query_time_secs; }
+    int CloserThanTolerance() { return closer_than_tolerance; }
+    PQP_REAL Distance() { return distance; }
+    const PQP_REAL *P1() { return p1; }
+    const PQP_REAL *P2() { return p2; }
+};
+
+/* C2A_DistanceResult's public face (the closest pair as triangles and ids) */
+class C2A_DistanceResult {
+  public:
+    int num_bv_tests = 0, num_tri_tests = 0;
+    double query_time_secs = 0;
+    PQP_REAL R[3][3] = {}, T[3] = {};
+    PQP_REAL rel_err = 0, abs_err = 0, distance = 0, p1[3] = {}, p2[3] = {};
+    int qsize = 2;
+    Tri *last_triA = nullptr, *last_triB = nullptr;
+    int t1 = -1, t2 = -1; /* caller ids of the closest pair */
+    int NumBVTests() { return num_bv_tests; }
+    int NumTriTests() { return num_tri_tests; }
+    double QueryTimeSecs() { return query_time_secs; }
+    PQP_REAL Distance() { return distance; }
+    const PQP_REAL *P1() { return p1; }
+    const PQP_REAL *P2() { return p2; }
+};
+
+/* The exact distance (rel_err = abs_err = 0 only; other values return
+ * C2A_ERR_INVALID_ARGUMENT), seeded with o1->last_tri / o2->last_tri; the
+ * closest pair comes back in result->last_triA/B (the models are not
+ * changed).  Returns 0 (PQP_OK) or a c2a_status. */
+int C2A_Distance(C2A_DistanceResult *result, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                 PQP_REAL T2[3], C2A_Model *o2, PQP_REAL rel_err, PQP_REAL abs_err, int qsize = 2);
+
+/* Is any triangle pair within `tolerance`? (qsize 2: the depth-first order
+ * with the closer child first, stopping at the first such pair) */
+int C2A_Tolerance(PQP_ToleranceResult *res, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                  PQP_REAL T2[3], C2A_Model *o2, PQP_REAL tolerance, int qsize = 2);
+
+/* The contacting triangle pairs (all, or the first found) */
+int C2A_Collide(PQP_CollideResult *result, PQP_REAL R1[3][3], PQP_REAL T1[3], C2A_Model *o1, PQP_REAL R2[3][3],
+                PQP_REAL T2[3], C2A_Model *o2, int flag = C2A_ALL_CONTACTS);
 
 /* One query of C2A_SolveBatch: the four poses of C2A_Solve and the seed pair
  * (dres.last_triA/B); seed < 0 means the model's last_tri. */

@@ -43,6 +43,11 @@ extern "C" {
 c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias, int32_t M, int32_t N, int32_t K,
                         int32_t flags, float *out_f32, uint16_t *out_bf16, void *stream);
 
+/* Synchronises the stream and reports whether any GEMM since the last check
+ * ran out of a bounded wait (C2A_ERR_CUDA; its output is then undefined);
+ * clears the record. */
+c2a_status c2a_mlp_check(void *stream);
+
 /* out (cols x rows) = in (rows x cols) transposed, bf16; rows, cols multiples of 32 */
 c2a_status c2a_mlp_transpose(const uint16_t *in, int32_t rows, int32_t cols, uint16_t *out, void *stream);
 

@@ -177,3 +177,51 @@ def test_static_queries_reject_bad_models(gpu_ctx):
     r, _ = gpu_ctx.collide(q, P, 1, 4, check=False)
     assert r["status"][0] == api.QUERY_BAD_INPUT
     assert len(gpu_ctx.tolerance(q[:0], P[:0], 0.1)) == 0
+
+
+@pytest.mark.gpu
+def test_cpp_dropin_static_queries_match_reference_fixture(lib, port):
+    """C2A_Tolerance, C2A_Collide and C2A_Distance of the C++ drop-in
+    (include/c2a_gb300_cpp.h) on the fixture's 96 pairs: the reference's
+    outputs, and the oracle's distance."""
+    import os
+    import subprocess
+
+    from c2a_gb300 import build
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = os.path.join(build.OUT_DIR, "static_dropin")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "cpp", "static_dropin.cpp"), "-o", exe, build.LIB,
+                    f"-Wl,-rpath,{build.OUT_DIR}"], check=True)
+    z = np.load(f"{GOLDEN}/static_queries_ref.npz")
+    ms = _meshes_of(z)
+    inp = os.path.join(build.OUT_DIR, "static_dropin.bin")
+    with open(inp, "wb") as fh:
+        np.array([len(ms)], np.int32).tofile(fh)
+        for m in ms:
+            np.array([len(m.verts), m.num_tris], np.int32).tofile(fh)
+            m.verts.astype(np.float64).tofile(fh)
+            m.faces.astype(np.int32).tofile(fh)
+        np.array([len(z["ab"])], np.int32).tofile(fh)
+        for i, (a, b) in enumerate(z["ab"]):
+            np.array([a, b], np.int32).tofile(fh)
+            z["R"][i].astype(np.float64).tofile(fh)
+            z["T"][i].astype(np.float64).tofile(fh)
+            np.array([z["tol"][i]], np.float64).tofile(fh)
+    lines = subprocess.run([exe, inp], check=True, capture_output=True, text=True).stdout.strip().split("\n")
+    assert len(lines) == 3 * len(z["ab"])
+    models = port.models(ms)
+    offs = z["pair_offsets"]
+    for i, (a, b) in enumerate(z["ab"]):
+        t = lines[3 * i].split()
+        e = z["tol_out"][i]
+        assert int(t[0]) == z["closer"][i] and (int(t[8]), int(t[9])) == (int(e[7]), int(e[8])), i
+        if int(t[0]):
+            assert [float(x) for x in t[1:8]] == e[:7].tolist(), i
+        c = list(map(int, lines[3 * i + 1].split()))
+        assert c[0] == offs[i + 1] - offs[i] and (c[1], c[2]) == tuple(z["collide_counts"][i]), i
+        assert np.array_equal(np.array(c[3:], np.int32).reshape(-1, 2), z["pairs"][offs[i]:offs[i + 1]]), i
+        d = lines[3 * i + 2].split()
+        pd, _, _ = port.distance(models, a, b, z["R"][i], z["T"][i], 0, 0)
+        assert float(d[0]) == pd, i
