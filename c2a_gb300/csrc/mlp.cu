@@ -585,7 +585,7 @@ int grid_for(int64_t count, int threads)
 extern "C" {
 
 #ifndef C2A_MLP_TCGEN05
-#define C2A_MLP_TCGEN05 0 /* 1: c2a_mlp_gemm runs k_gemm_tc */
+#define C2A_MLP_TCGEN05 1 /* 1: c2a_mlp_gemm runs k_gemm_tc (tcgen05, TMEM); 0: k_gemm (mma.sync) */
 #endif
 
 c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias, int32_t M, int32_t N, int32_t K,
