@@ -14,6 +14,7 @@
  * sums, Adam, the input assembly and its embedding scatter, top-k) is
  * bandwidth-bound elementwise or row-wise work.
  */
+#include <cuda.h> /* CUtensorMap and its enums; the encoder is reached through the runtime's entry-point query */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -379,6 +380,148 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const uint16_t *__restri
     }
 }
 
+/* ----------------------------------------- GEMM on tcgen05 fed by TMA */
+
+/* The production form of the same product: the tiles arrive by TMA
+ * (cp.async.bulk.tensor, 128-byte swizzle, out-of-range K filled with zeros)
+ * into three shared-memory stages; one thread issues the TMA copies, one
+ * thread the tcgen05.mma (the same 128 x 128 x 16 bf16 -> FP32 instruction,
+ * SWIZZLE_128B K-major descriptors: 8-row groups 1 KiB apart, the K = 16
+ * sub-steps 32 bytes apart inside the 128-byte swizzle atom), with full/empty
+ * mbarriers per stage between them; all four warps then read the
+ * accumulator from tensor memory.  Two CTAs fit an SM (100 KiB of shared
+ * memory, 128 TMEM columns each). */
+constexpr int kTmStages = 3;
+constexpr int kTmStageA = kTcM * kTcK * 2, kTmStageB = kTcN * kTcK * 2; /* 16 KiB each */
+constexpr int kTmSmem = kTmStages * (kTmStageA + kTmStageB) + 2048;     /* + barriers and 1 KiB alignment */
+
+__device__ __forceinline__ uint64_t tm_desc(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                 "[%4];\n" ::"r"(dst),
+                 "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_gemm_tma(const __grid_constant__ CUtensorMap tmA,
+                                                         const __grid_constant__ CUtensorMap tmB,
+                                                         const float *__restrict__ bias, int M, int N, int K,
+                                                         int flags, float *__restrict__ out_f32,
+                                                         uint16_t *__restrict__ out_bf16, int *__restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char tm_raw[];
+    const uint32_t raw = smem_u32(tm_raw);
+    unsigned char *base = tm_raw + ((1024u - (raw & 1023u)) & 1023u); /* swizzle atoms need 1 KiB alignment */
+    const uint32_t sA = smem_u32(base), sB = sA + kTmStages * kTmStageA;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base + kTmStages * (kTmStageA + kTmStageB));
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kTmStages + 1);
+    const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * kTmStages, done = full0 + 16 * kTmStages;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kTmStages; s++) {
+            mbar_init(full0 + 8 * s, 1);
+            mbar_init(empty0 + 8 * s, 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)&tmA) : "memory");
+        asm volatile("prefetch.tensormap [%0];\n" ::"l"((uint64_t)&tmB) : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"((uint32_t)kTcN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    const int steps = (K + kTcK - 1) / kTcK;
+    bool ok = true;
+    if (warp == 0 && lane == 0) { /* producer: TMA copies into a stage once its last MMAs are done */
+        for (int kt = 0; kt < steps; kt++) {
+            const int s = kt % kTmStages, use = kt / kTmStages;
+            if (use >= 1) ok = mbar_wait(empty0 + 8 * s, (uint32_t)((use - 1) & 1)) && ok;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full0 + 8 * s),
+                         "r"((uint32_t)(kTmStageA + kTmStageB))
+                         : "memory");
+            tma_load_2d(sA + s * kTmStageA, &tmA, kt * kTcK, m0, full0 + 8 * s);
+            tma_load_2d(sB + s * kTmStageB, &tmB, kt * kTcK, n0, full0 + 8 * s);
+        }
+    } else if (warp == 1 && lane == 0) { /* MMA issuer */
+        for (int kt = 0; kt < steps; kt++) {
+            const int s = kt % kTmStages, use = kt / kTmStages;
+            ok = mbar_wait(full0 + 8 * s, (uint32_t)(use & 1)) && ok;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t a0 = sA + s * kTmStageA, b0 = sB + s * kTmStageB;
+#pragma unroll
+            for (int kk = 0; kk < kTcK / 16; kk++)
+                tc_mma(tmem, tm_desc(a0 + 32 * kk), tm_desc(b0 + 32 * kk), (kt > 0 || kk > 0) ? 1u : 0u);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             empty0 + 8 * s)
+                         : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(done)
+                     : "memory");
+    }
+    __syncwarp();
+    ok = mbar_wait(done, 0u) && ok;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    const int row = m0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcN; c0 += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                     "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+                     "[%32];\n"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                       "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                       "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                       "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (row < M) {
+#pragma unroll
+            for (int j = 0; j < 32; j += 2) {
+                const int col = n0 + c0 + j;
+                float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
+                if (flags & C2A_MLP_BIAS) {
+                    v0 += bias[col];
+                    v1 += bias[col + 1];
+                }
+                const size_t o = (size_t)row * N + col;
+                if (out_f32) *reinterpret_cast<float2 *>(out_f32 + o) = make_float2(v0, v1);
+                if (out_bf16) {
+                    if (flags & C2A_MLP_GELU) {
+                        v0 = gelu(v0);
+                        v1 = gelu(v1);
+                    }
+                    *reinterpret_cast<uint32_t *>(out_bf16 + o) = (uint32_t)f2bf(v0) | ((uint32_t)f2bf(v1) << 16);
+                }
+            }
+        }
+    }
+    if (!ok) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"((uint32_t)kTcN));
+    }
+}
+
 /* ------------------------------------------------------ elementwise/rows */
 
 __global__ void k_transpose(const uint16_t *__restrict__ in, int rows, int cols, uint16_t *__restrict__ out)
@@ -585,14 +728,52 @@ int grid_for(int64_t count, int threads)
 extern "C" {
 
 #ifndef C2A_MLP_TCGEN05
-#define C2A_MLP_TCGEN05 1 /* 1: c2a_mlp_gemm runs k_gemm_tc (tcgen05, TMEM); 0: k_gemm (mma.sync) */
+#define C2A_MLP_TCGEN05 1 /* 2: k_gemm_tma; 1: k_gemm_tc (tcgen05, TMEM); 0: k_gemm (mma.sync) */
 #endif
+typedef CUresult (*PFN_encode_tiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                     const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias, int32_t M, int32_t N, int32_t K,
                         int32_t flags, float *out_f32, uint16_t *out_bf16, void *stream)
 {
     if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % kBM || N % kBN || K % kBK || ((flags & C2A_MLP_BIAS) && !bias))
         return C2A_ERR_INVALID_ARGUMENT;
+    if (C2A_MLP_TCGEN05 == 2) {
+        static PFN_encode_tiled encode = nullptr;
+        static bool attr = false;
+        if (!encode) {
+            void *fn = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                    cudaSuccess ||
+                q != cudaDriverEntryPointSuccess || !fn)
+                return C2A_ERR_CUDA;
+            encode = (PFN_encode_tiled)fn;
+        }
+        if (!attr) {
+            if (cudaFuncSetAttribute(k_gemm_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem) != cudaSuccess)
+                return C2A_ERR_CUDA;
+            attr = true;
+        }
+        CUtensorMap ta, tb;
+        const cuuint64_t da[2] = {(cuuint64_t)K, (cuuint64_t)M}, db[2] = {(cuuint64_t)K, (cuuint64_t)N};
+        const cuuint64_t stride[1] = {(cuuint64_t)K * 2};
+        const cuuint32_t box[2] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM}, es[2] = {1, 1};
+        if (encode(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)A, da, stride, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+            encode(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)B, db, stride, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return C2A_ERR_INVALID_ARGUMENT;
+        int *err = nullptr;
+        if (cudaGetSymbolAddress((void **)&err, g_tc_err) != cudaSuccess) return C2A_ERR_CUDA;
+        const dim3 grid(N / kTcN, M / kTcM);
+        k_gemm_tma<<<grid, kTcThreads, kTmSmem, (cudaStream_t)stream>>>(ta, tb, bias, M, N, K, flags, out_f32,
+                                                                         out_bf16, err);
+        return launch_status();
+    }
     if (C2A_MLP_TCGEN05) {
         static bool attr = false;
         if (!attr) {
