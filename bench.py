@@ -73,6 +73,11 @@ def parse():
                         "queries (costs measured by the library) starts the costliest queries first; geometric: "
                         "queries whose bounding spheres approach first.  Results are identical either way.")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", choices=["config2", "config4"], default="config2",
+                   help="config4: config 2 plus --near grazing near-contact queries (gap log-uniform [1e-6, 1e-3] "
+                        "diag, velocity within 5 degrees of the tangent plane); reports the exact distance at "
+                        "every near-contact TOC against th_ca")
+    p.add_argument("--near", type=int, default=16384, help="--workload config4: near-contact queries")
     return p.parse_args()
 
 
@@ -242,6 +247,35 @@ def run_learned(args, rank, world, local):
     r = learned.experiment(n_train=args.train, n_eval=args.queries, epochs=args.epochs, pool=12,
                            tri_range=(1000, 200000), engine=api.ENGINE_BATCHED, seed=3,
                            log=lambda m: print(m, file=sys.stderr, flush=True))
+    ev, rp = r.pop("eval_workload"), r.pop("eval_results")
+    # roofline of the hinted batch on the FP64 pipe: the reference counters' node-pair and triangle tests at the
+    # per-unit flops of the REFERENCE path (the closest-pair search's node pairs are not in those counters, so
+    # this understates the work)
+    bv, tri = int(r["bv_tests_hinted"]), int(rp["num_tri_tests"].sum())
+    fma_peak, add_peak = api.fp64_peak(local)
+    achieved = (bv * F_BV + tri * F_TRI) / (r["hinted_ms"] / 1e3) / 1e9
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": fma_peak / 1e9, "unit": "GFLOP/s",
+                "frac": achieved / (fma_peak / 1e9), "traffic": None, "peak_unfused": add_peak / 1e9,
+                "peak_source": "measured in this run: c2a_probe_fp64_peak", "kernel": "k_dsearch + step waves",
+                "note": "counts only the step's node-pair and triangle tests (num_bv_tests, num_tri_tests); the "
+                        "closest-pair search that seeds every step is not in those counters"}
+    cpu = None
+    if not args.no_cpu:  # the oracle port in CANONICAL mode on an evenly strided sample of the held-out batch
+        idx = strided(ev.n, args.cpu_sample or 4096)
+        ev.params.update(mode=api.MODE_CANONICAL)
+        rate, dt, pres, _ = cpu_baseline(ev, idx, os.cpu_count() or 1)
+        fields = ("collisionfree", "numCA", "toc", "distance", "mint", "num_bv_tests", "num_tri_tests",
+                  "num_contact", "R_toc", "T_toc")
+        cpu = {"value": rate, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"{len(idx)} of the {ev.n} held-out queries, evenly strided, CANONICAL mode "
+                         f"({dt:.1f} s wall)",
+               "bit_identical_to_gpu": bool(all(pres[f].tobytes() == rp[f][idx].tobytes() for f in fields)),
+               "compared": "every result field but the reported seed pair (among exact ties the GPU reports the "
+                           "smallest pair)"}
+    e2e = {"value": args.queries / r["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": r["e2e_h2d_bytes"],
+           "d2h_bytes_per_step": r["e2e_d2h_bytes"], "identical_results": r["e2e_identical"],
+           "api": "features on the host, the network's top-k on the device, c2a_solve_batch_hinted from host "
+                  "arrays (learned.solve_hinted)"}
     line = {"metric": METRIC, "value": r["hinted_qps"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": r["hinted_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64 CA / bf16 network", "impl": "learned",
@@ -255,7 +289,7 @@ def run_learned(args, rank, world, local):
             "true_pair_hint_qps": args.queries / r["oracle_hint_ms"] * 1e3,
             "top1": r["top1"], "top8": r["topk"], "train_loss": r["loss"], "label_s": r["label_s"],
             "train_s": r["train_s"], "wall_s": time.time() - t0, "colliding": r["colliding"],
-            "e2e": None, "roofline": None, "cpu_baseline": None, "gpu_launches": None}
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": r["e2e_launches"]}
     print(json.dumps(line), flush=True)
 
 
@@ -285,10 +319,15 @@ def main():
         build.build()
     if dist:
         dist.barrier()
-    wl = workloads.config2(n=args.queries, seed=2 + rank, device=f"cuda:{local}")
+    ctx = api.Context(local)
+    if args.workload == "config4":  # the near-contact placement runs the library's exact distance query
+        knot = workloads.config2(n=1, seed=2, device=f"cuda:{local}").meshes[0]
+        wl = workloads.config4(workloads.gpu_distance_fn(ctx, ctx.model(knot)), n=args.queries, n_near=args.near,
+                               seed=4 + rank, device=f"cuda:{local}")
+    else:
+        wl = workloads.config2(n=args.queries, seed=2 + rank, device=f"cuda:{local}")
     wl.params["mode"] = 1 if args.mode == "canonical" else 0
     wl.params["engine"] = ENGINES[args.engine]
-    ctx = api.Context(local)
     mid = ctx.model(wl.meshes[0])
     qint = wl.qint.copy()
     qint[:, :2] = mid
@@ -485,6 +524,29 @@ def main():
                "api": ("c2a_solve_batch_ordered_host (host buffers; the order from the network on the device)"
                        if h2d_extra else "c2a_solve_batch (host buffers)")}
 
+    near_info = None
+    if args.workload == "config4":
+        # the near-contact part: bit-identical to the reference (the CPU sample below covers it), so no TOC is
+        # later than the reference's; and where the CA loop reached tolerance_d (numCA >= 2), the exact distance
+        # at the returned TOC poses must be within th_ca
+        nr = res[args.queries:]
+        hit = (nr["collisionfree"] == 0) & (nr["distance"] <= wl.params["tol_d"]) & (nr["numCA"] >= 2) & \
+              (nr["distance"] > 0)
+        P = np.zeros((int(hit.sum()), workloads.POSE_WIDTH))
+        P[:, 0:9] = nr["R_toc"][hit, 0]
+        P[:, 9:12] = nr["T_toc"][hit, 0]
+        P[:, 24:33] = nr["R_toc"][hit, 1]
+        P[:, 33:36] = nr["T_toc"][hit, 1]
+        dq = qint[args.queries:][hit].copy()
+        dq[:, 2] = nr["seed_a"][hit]
+        dq[:, 3] = nr["seed_b"][hit]
+        exact = ctx.distance(dq, P)["distance"] if len(dq) else np.zeros(0)
+        near_info = {"queries": int(len(nr)), "colliding": int((nr["collisionfree"] == 0).sum()),
+                     "toc_checked": int(hit.sum()), "max_exact_distance_at_toc": float(exact.max()) if len(exact)
+                     else None, "th_ca": wl.params["th_ca"],
+                     "all_within_th_ca": bool((exact <= wl.params["th_ca"] * (1 + 1e-12)).all()),
+                     "toc_error_vs_reference": "0 (bit-identical: see cpu_baseline.bit_identical_to_gpu)"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -512,7 +574,7 @@ def main():
                 "config": config_dict(wl, args), "implementation": implementation_dict(args, run_engine), "clocks": clk,
                 "gpu_launches": launches, "e2e": e2e,
                 "roofline": roofline, "cpu_baseline": cpu,
-                "learned_order": learned_info, "tuned_launch": tuned,
+                "learned_order": learned_info, "tuned_launch": tuned, "near_contact": near_info,
                 "collision_fraction": float(1 - res["collisionfree"].mean()),
                 "mean_numCA": float(res["numCA"].mean()), "step_ms": step_ms}
         print(json.dumps(line), flush=True)

@@ -492,23 +492,33 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tma(const __grid_constant__
                        "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                      : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (row < M) {
+        if (row < M) { /* this row's 32 columns in 16-byte stores */
 #pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-                const int col = n0 + c0 + j;
-                float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
-                if (flags & C2A_MLP_BIAS) {
-                    v0 += bias[col];
-                    v1 += bias[col + 1];
+            for (int g = 0; g < 32; g += 8) {
+                const int col = n0 + c0 + g;
+                float x[8];
+#pragma unroll
+                for (int e = 0; e < 8; e++) {
+                    x[e] = __uint_as_float(v[g + e]);
+                    if (flags & C2A_MLP_BIAS) x[e] += bias[col + e];
                 }
                 const size_t o = (size_t)row * N + col;
-                if (out_f32) *reinterpret_cast<float2 *>(out_f32 + o) = make_float2(v0, v1);
+                if (out_f32) {
+                    reinterpret_cast<float4 *>(out_f32 + o)[0] = make_float4(x[0], x[1], x[2], x[3]);
+                    reinterpret_cast<float4 *>(out_f32 + o)[1] = make_float4(x[4], x[5], x[6], x[7]);
+                }
                 if (out_bf16) {
-                    if (flags & C2A_MLP_GELU) {
-                        v0 = gelu(v0);
-                        v1 = gelu(v1);
+                    uint32_t w[4];
+#pragma unroll
+                    for (int e = 0; e < 8; e += 2) {
+                        float a = x[e], b = x[e + 1];
+                        if (flags & C2A_MLP_GELU) {
+                            a = gelu(a);
+                            b = gelu(b);
+                        }
+                        w[e / 2] = (uint32_t)f2bf(a) | ((uint32_t)f2bf(b) << 16);
                     }
-                    *reinterpret_cast<uint32_t *>(out_bf16 + o) = (uint32_t)f2bf(v0) | ((uint32_t)f2bf(v1) << 16);
+                    *reinterpret_cast<uint4 *>(out_bf16 + o) = make_uint4(w[0], w[1], w[2], w[3]);
                 }
             }
         }

@@ -483,6 +483,20 @@ def experiment(n_train: int = 2_000_000, n_eval: int = 65536, epochs: int = 4, p
                    bv_tests_plain=int(rp["num_bv_tests"].sum()), bv_tests_hinted=int(rh["num_bv_tests"].sum()))
         log(f"CANONICAL engine {engine}: plain {ms_plain:.1f} ms, hinted {ms_hint:.1f} ms "
             f"({out['speedup']:.3f}x), identical results: {out['identical']}")
+        # end to end from host arrays: pose features on the host, the network's top-k on the device, the
+        # hint codes, then the hinted solve (queries and hints H2D, results and contacts D2H)
+        launches0 = ctx.launches()
+        t3 = time.perf_counter()
+        f_ev = features(wl.poses[ev], diag[wl.qint[ev, 0]], diag[wl.qint[ev, 1]])
+        top_e = net.topk(f_ev, wl.qint[ev, 0], wl.qint[ev, 1], k)
+        re, _ = solve_hinted(ctx, q[ev], wl.poses[ev], prm, hints_of(top_e, q[ev], tab), cpq)
+        out["e2e_s"] = time.perf_counter() - t3
+        out["e2e_launches"] = ctx.launches() - launches0
+        out["e2e_identical"] = all(re[f].tobytes() == rp[f].tobytes() for f in fields)
+        out["e2e_h2d_bytes"] = n_eval * (api.QUERY_DTYPE.itemsize + 18 * 4 + 2 * 4 + k * 8)
+        out["e2e_d2h_bytes"] = n_eval * (api.RESULT_DTYPE.itemsize + cpq * api.CONTACT_DTYPE.itemsize + k * 4)
+        out["eval_results"] = rp
+        out["eval_workload"] = wl.subset(np.arange(n_train, n_train + n_eval))
     return out
 
 
