@@ -1,14 +1,10 @@
 /*
  * mlp.cu -- the learned seeding's network kernels (include/c2a_mlp.h).
  *
- * GEMM: out = A B^T with A (M x K) and B (N x K) in bf16, K contiguous, on
- * the tensor cores (mma.sync m16n8k16, bf16 in, FP32 accumulate).  A block
- * computes a 128 x 128 tile with eight warps (2 x 4, 64 x 32 each); K moves
- * in steps of 32 through a double-buffered shared-memory stage filled with
- * 16-byte cp.async copies, fragments come from ldmatrix.  Rows are padded to
- * 80 bytes so that the eight row addresses of an ldmatrix hit eight different
- * 16-byte bank groups.  The epilogue adds the bias and applies GELU (erff,
- * called) in registers and writes FP32 and/or bf16.
+ * GEMM: out = A B^T on tcgen05 with the accumulator in tensor memory, the
+ * operands brought in by TMA (k_gemm_tma; the layout and the pipeline are
+ * described above the kernel).  The epilogue adds the bias and applies GELU
+ * (erff, called) in registers and writes FP32 and/or bf16.
  *
  * Everything else (transposes, GELU backward, softmax cross-entropy, column
  * sums, Adam, the input assembly and its embedding scatter, top-k) is
@@ -45,158 +41,26 @@ __device__ __forceinline__ float gelu_grad(float x)
 
 /* ------------------------------------------------------------------ GEMM */
 
-constexpr int kBM = 128, kBN = 128, kBK = 32;
-constexpr int kRowH = kBK + 8; /* bf16 per shared-memory row (80 bytes) */
-constexpr int kGemmThreads = 256;
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
-__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::); }
-
-__device__ __forceinline__ void ldmatrix_x4(uint32_t r[4], const void *smem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(s));
-}
-
-__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1)
-{
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
-                 "{%8, %9}, {%0, %1, %2, %3};\n"
-                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-/* one K-step of the A and B tiles into stage buffers (each thread: two 16-byte
- * chunks of A, two of B; a tile row is 32 bf16 = four chunks) */
-__device__ __forceinline__ void load_stage(const uint16_t *A, const uint16_t *B, int K, int m0, int n0, int k0,
-                                           uint16_t *sA, uint16_t *sB)
-{
-#pragma unroll
-    for (int i = 0; i < 2; i++) {
-        const int c = threadIdx.x + i * kGemmThreads; /* 0..511 */
-        const int row = c >> 2, col = (c & 3) * 8;
-        cp_async16(sA + row * kRowH + col, A + (size_t)(m0 + row) * K + k0 + col);
-        cp_async16(sB + row * kRowH + col, B + (size_t)(n0 + row) * K + k0 + col);
-    }
-}
-
-__global__ void __launch_bounds__(kGemmThreads) k_gemm(const uint16_t *__restrict__ A, const uint16_t *__restrict__ B,
-                                                       const float *__restrict__ bias, int M, int N, int K,
-                                                       int flags, float *__restrict__ out_f32,
-                                                       uint16_t *__restrict__ out_bf16)
-{
-    __shared__ __align__(16) uint16_t sA[2][kBM * kRowH];
-    __shared__ __align__(16) uint16_t sB[2][kBN * kRowH];
-    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32; /* this warp's 64 x 32 sub-tile */
-    float acc[4][4][4];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.0f;
-
-    const int steps = K / kBK;
-    load_stage(A, B, K, m0, n0, 0, sA[0], sB[0]);
-    cp_async_commit();
-    for (int s = 0; s < steps; s++) {
-        const int cur = s & 1;
-        if (s + 1 < steps) {
-            load_stage(A, B, K, m0, n0, (s + 1) * kBK, sA[cur ^ 1], sB[cur ^ 1]);
-            cp_async_commit();
-            cp_async_wait1();
-        } else {
-            cp_async_wait0();
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kBK; kk += 16) {
-            uint32_t af[4][4], bfr[2][4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) { /* A rows wm + 16 i .. + 15, k kk .. kk + 15 */
-                const int r = wm + 16 * i + (lane & 15), c = kk + (lane >> 4) * 8;
-                ldmatrix_x4(af[i], sA[cur] + r * kRowH + c);
-            }
-#pragma unroll
-            for (int j = 0; j < 2; j++) { /* B rows (n) wn + 16 j .. + 15 */
-                const int r = wn + 16 * j + (lane & 7) + ((lane >> 4) << 3), c = kk + ((lane >> 3) & 1) * 8;
-                ldmatrix_x4(bfr[j], sB[cur] + r * kRowH + c);
-            }
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j >> 1][(j & 1) * 2], bfr[j >> 1][(j & 1) * 2 + 1]);
-        }
-        __syncthreads();
-    }
-    /* epilogue: c0, c1 at (row g, cols 2 t, 2 t + 1), c2, c3 at row g + 8 */
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int row = m0 + wm + 16 * i + g + 8 * h, col = n0 + wn + 8 * j + 2 * t;
-                float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
-                if (flags & C2A_MLP_BIAS) {
-                    v0 += bias[col];
-                    v1 += bias[col + 1];
-                }
-                const size_t o = (size_t)row * N + col;
-                if (out_f32) *reinterpret_cast<float2 *>(out_f32 + o) = make_float2(v0, v1);
-                if (out_bf16) {
-                    if (flags & C2A_MLP_GELU) {
-                        v0 = gelu(v0);
-                        v1 = gelu(v1);
-                    }
-                    *reinterpret_cast<uint32_t *>(out_bf16 + o) = (uint32_t)f2bf(v0) | ((uint32_t)f2bf(v1) << 16);
-                }
-            }
-}
-
-/* --------------------------------------------------- GEMM on tcgen05 */
-
-/* The same product on the fifth-generation tensor cores: a 128 x 128 output
- * tile per CTA of four warps, the FP32 accumulator in tensor memory (128
- * columns), K in steps of 64 through two shared-memory stages in the
- * canonical no-swizzle K-major layout (8-row x 16-byte core matrices: the two
- * K-neighbours of a core matrix 128 bytes apart (LBO), the M/N-neighbours 1 KiB
- * apart (SBO)), filled with 16-byte cp.async copies while the tensor core
- * works on the other stage.  One thread issues four tcgen05.mma (M 128, N 128,
- * K 16, bf16 x bf16 -> FP32) per stage and commits them to the stage's
- * mbarrier; the epilogue reads the accumulator with tcgen05.ld (warp w: rows
- * 32 w .. 32 w + 31, one row per thread) and applies bias and GELU as the
- * mma.sync kernel does.  Every mbarrier wait is bounded: a wait that runs
- * out sets *err and the CTA still releases its tensor memory. */
+/* out = A B^T with A (M x K) and B (N x K) bf16, K contiguous, on the
+ * fifth-generation tensor cores.  A CTA of four warps owns a 128 x 128 output
+ * tile; its FP32 accumulator lives in 128 columns of tensor memory
+ * (tcgen05.alloc).  The A and B tiles arrive by TMA (cp.async.bulk.tensor
+ * with 128-byte swizzle; K past the end is filled with zeros) in steps of 64
+ * into three shared-memory stages; one thread issues the TMA copies, another
+ * the tcgen05.mma (M 128, N 128, K 16, bf16 x bf16 -> FP32; SWIZZLE_128B
+ * K-major descriptors: 8-row groups 1 KiB apart, the K = 16 sub-steps 32 bytes
+ * apart inside the 128-byte swizzle atom), with a full and an empty mbarrier
+ * per stage between them (tcgen05.commit arms the empty one).  After the last
+ * commit all four warps read the accumulator with tcgen05.ld (warp w: rows
+ * 32 w .. 32 w + 31, one row per thread), add the bias, apply GELU and write
+ * FP32 and/or bf16 in 16-byte stores.  Two CTAs fit an SM (100 KiB of shared
+ * memory, 128 TMEM columns each).  Every mbarrier wait is bounded by the
+ * global timer: a wait that runs out records an error (c2a_mlp_check) and the
+ * CTA still releases its tensor memory. */
 constexpr int kTcM = 128, kTcN = 128, kTcK = 64, kTcThreads = 128;
-constexpr int kTcStageBytes = (kTcM + kTcN) * kTcK * 2; /* 32 KiB: A tile then B tile */
-constexpr int kTcSmem = 2 * kTcStageBytes + 1024;      /* two stages + barriers; 4 CTAs per SM at most */
-constexpr uint32_t kTcLBO = 128, kTcSBO = 1024; /* memory strides: K-neighbour, M/N-neighbour core matrices */
-#ifndef C2A_TC_SWAP
-#define C2A_TC_SWAP 0 /* 1: the descriptor's two offset fields exchanged */
-#endif
-constexpr uint32_t kTcDescL = C2A_TC_SWAP ? kTcSBO : kTcLBO, kTcDescS = C2A_TC_SWAP ? kTcLBO : kTcSBO;
-__device__ int g_tc_err; /* set when a bounded mbarrier wait of k_gemm_tc ran out */
+__device__ int g_tc_err; /* set when a bounded mbarrier wait of k_gemm_tma ran out */
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-/* shared-memory matrix descriptor: start, LBO, SBO (all >> 4), version 1, no swizzle */
-__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr)
-{
-    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((kTcDescL >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((kTcDescS >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
 
 /* instruction descriptor of kind::f16: FP32 accumulator, bf16 A and B, both K-major, N 128, M 128 */
 constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcN >> 3) << 17) |
@@ -241,156 +105,6 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t b
                  ::"r"(tmem), "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(accumulate));
 }
 
-/* one stage: rows of A and B (K-chunks of 16 bytes) into the core-matrix layout; chunks past K are zero */
-__device__ __forceinline__ void tc_load_stage(const uint16_t *A, const uint16_t *B, int K, int m0, int n0, int k0,
-                                              unsigned char *stage)
-{
-#pragma unroll 4
-    for (int c = threadIdx.x; c < (kTcM + kTcN) * (kTcK / 8); c += kTcThreads) {
-        const int row = c >> 3, kc = c & 7; /* row 0..255 (A then B), 16-byte chunk along K */
-        const bool isB = row >= kTcM;
-        const int r = isB ? row - kTcM : row;
-        unsigned char *dst = stage + (isB ? kTcM * kTcK * 2 : 0) + (r >> 3) * kTcSBO + kc * kTcLBO + (r & 7) * 16;
-        const int k = k0 + kc * 8;
-        if (k < K) {
-            const uint16_t *src = isB ? B + (size_t)(n0 + r) * K + k : A + (size_t)(m0 + r) * K + k;
-            cp_async16(dst, src);
-        } else {
-            *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(const uint16_t *__restrict__ A, const uint16_t *__restrict__ B,
-                                                        const float *__restrict__ bias, int M, int N, int K, int flags,
-                                                        float *__restrict__ out_f32, uint16_t *__restrict__ out_bf16,
-                                                        int *__restrict__ err)
-{
-    extern __shared__ __align__(1024) unsigned char tc_smem[];
-    unsigned char *stage0 = tc_smem, *stage1 = tc_smem + kTcStageBytes;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(tc_smem + 2 * kTcStageBytes);
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tc_smem + 2 * kTcStageBytes + 64);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.y * kTcM, n0 = blockIdx.x * kTcN;
-    const uint32_t bar0 = smem_u32(&bars[0]), bar1 = smem_u32(&bars[1]);
-
-    if (threadIdx.x == 0) {
-        mbar_init(bar0, 1);
-        mbar_init(bar1, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
-                     "r"((uint32_t)kTcN));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *tmem_slot;
-
-    const int steps = (K + kTcK - 1) / kTcK;
-    bool ok = true;
-    uint32_t phase[2] = {0u, 0u};
-    tc_load_stage(A, B, K, m0, n0, 0, stage0);
-    cp_async_commit();
-    for (int s = 0; s < steps; s++) {
-        unsigned char *cur = (s & 1) ? stage1 : stage0;
-        unsigned char *nxt = (s & 1) ? stage0 : stage1;
-        if (s + 1 < steps) {
-            if (s >= 1) { /* the MMAs of step s - 1 read the other stage: wait for them before refilling it */
-                const int o = (s - 1) & 1;
-                ok = mbar_wait(o ? bar1 : bar0, phase[o]) && ok;
-                phase[o] ^= 1u;
-            }
-            tc_load_stage(A, B, K, m0, n0, (s + 1) * kTcK, nxt);
-            cp_async_commit();
-            cp_async_wait1();
-        } else {
-            cp_async_wait0();
-        }
-        /* this thread's copies into the current stage are done: publish them to the tensor core's proxy */
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t a0 = smem_u32(cur), b0 = smem_u32(cur + kTcM * kTcK * 2);
-#pragma unroll
-            for (int kk = 0; kk < kTcK / 16; kk++) /* K 16 = two core matrices = 2 LBO further along K */
-                tc_mma(tmem, tc_desc(a0 + kk * 2 * kTcLBO), tc_desc(b0 + kk * 2 * kTcLBO), (s > 0 || kk > 0) ? 1u : 0u);
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             (s & 1) ? bar1 : bar0)
-                         : "memory");
-        }
-    }
-    /* the last commit covers every MMA issued before it */
-    {
-        const int o = (steps - 1) & 1;
-        ok = mbar_wait(o ? bar1 : bar0, phase[o]) && ok;
-        if (steps >= 2) { /* the other stage's last commit completed with it; keep the phases consistent */
-            const int p = (steps - 2) & 1;
-            if (p != o) ok = mbar_wait(p ? bar1 : bar0, phase[p]) && ok;
-        }
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-
-    /* epilogue: warp w owns accumulator rows 32 w .. 32 w + 31 (TMEM lanes), 32 columns per load */
-    const int row = m0 + 32 * warp + lane;
-#pragma unroll 1
-    for (int c0 = 0; c0 < kTcN; c0 += 32) {
-        uint32_t v[32];
-        const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
-                     "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
-                     "[%32];\n"
-                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                       "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                       "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                       "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                     : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (row < M) {
-#pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-                const int col = n0 + c0 + j;
-                float v0 = __uint_as_float(v[j]), v1 = __uint_as_float(v[j + 1]);
-                if (flags & C2A_MLP_BIAS) {
-                    v0 += bias[col];
-                    v1 += bias[col + 1];
-                }
-                const size_t o = (size_t)row * N + col;
-                if (out_f32) *reinterpret_cast<float2 *>(out_f32 + o) = make_float2(v0, v1);
-                if (out_bf16) {
-                    if (flags & C2A_MLP_GELU) {
-                        v0 = gelu(v0);
-                        v1 = gelu(v1);
-                    }
-                    *reinterpret_cast<uint32_t *>(out_bf16 + o) = (uint32_t)f2bf(v0) | ((uint32_t)f2bf(v1) << 16);
-                }
-            }
-        }
-    }
-    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    if (warp == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"((uint32_t)kTcN));
-    }
-}
-
-/* ----------------------------------------- GEMM on tcgen05 fed by TMA */
-
-/* The production form of the same product: the tiles arrive by TMA
- * (cp.async.bulk.tensor, 128-byte swizzle, out-of-range K filled with zeros)
- * into three shared-memory stages; one thread issues the TMA copies, one
- * thread the tcgen05.mma (the same 128 x 128 x 16 bf16 -> FP32 instruction,
- * SWIZZLE_128B K-major descriptors: 8-row groups 1 KiB apart, the K = 16
- * sub-steps 32 bytes apart inside the 128-byte swizzle atom), with full/empty
- * mbarriers per stage between them; all four warps then read the
- * accumulator from tensor memory.  Two CTAs fit an SM (100 KiB of shared
- * memory, 128 TMEM columns each). */
 constexpr int kTmStages = 3;
 constexpr int kTmStageA = kTcM * kTcK * 2, kTmStageB = kTcN * kTcK * 2; /* 16 KiB each */
 constexpr int kTmSmem = kTmStages * (kTmStageA + kTmStageB) + 2048;     /* + barriers and 1 KiB alignment */
@@ -737,9 +451,6 @@ int grid_for(int64_t count, int threads)
 
 extern "C" {
 
-#ifndef C2A_MLP_TCGEN05
-#define C2A_MLP_TCGEN05 1 /* 2: k_gemm_tma; 1: k_gemm_tc (tcgen05, TMEM); 0: k_gemm (mma.sync) */
-#endif
 typedef CUresult (*PFN_encode_tiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                      const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                      CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -747,59 +458,41 @@ typedef CUresult (*PFN_encode_tiled)(CUtensorMap *, CUtensorMapDataType, cuuint3
 c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias, int32_t M, int32_t N, int32_t K,
                         int32_t flags, float *out_f32, uint16_t *out_bf16, void *stream)
 {
-    if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % kBM || N % kBN || K % kBK || ((flags & C2A_MLP_BIAS) && !bias))
+    if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % kTcM || N % kTcN || K % 32 ||
+        ((flags & C2A_MLP_BIAS) && !bias) || ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
         return C2A_ERR_INVALID_ARGUMENT;
-    if (C2A_MLP_TCGEN05 == 2) {
-        static PFN_encode_tiled encode = nullptr;
-        static bool attr = false;
-        if (!encode) {
-            void *fn = nullptr;
-            cudaDriverEntryPointQueryResult q;
-            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-                    cudaSuccess ||
-                q != cudaDriverEntryPointSuccess || !fn)
-                return C2A_ERR_CUDA;
-            encode = (PFN_encode_tiled)fn;
-        }
-        if (!attr) {
-            if (cudaFuncSetAttribute(k_gemm_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem) != cudaSuccess)
-                return C2A_ERR_CUDA;
-            attr = true;
-        }
-        CUtensorMap ta, tb;
-        const cuuint64_t da[2] = {(cuuint64_t)K, (cuuint64_t)M}, db[2] = {(cuuint64_t)K, (cuuint64_t)N};
-        const cuuint64_t stride[1] = {(cuuint64_t)K * 2};
-        const cuuint32_t box[2] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM}, es[2] = {1, 1};
-        if (encode(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)A, da, stride, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
-            encode(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)B, db, stride, box, es,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-            return C2A_ERR_INVALID_ARGUMENT;
-        int *err = nullptr;
-        if (cudaGetSymbolAddress((void **)&err, g_tc_err) != cudaSuccess) return C2A_ERR_CUDA;
-        const dim3 grid(N / kTcN, M / kTcM);
-        k_gemm_tma<<<grid, kTcThreads, kTmSmem, (cudaStream_t)stream>>>(ta, tb, bias, M, N, K, flags, out_f32,
-                                                                         out_bf16, err);
-        return launch_status();
+    static PFN_encode_tiled encode = nullptr;
+    static bool attr = false;
+    if (!encode) { /* the driver's tensor-map encoder, reached through the runtime */
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return C2A_ERR_CUDA;
+        encode = (PFN_encode_tiled)fn;
     }
-    if (C2A_MLP_TCGEN05) {
-        static bool attr = false;
-        if (!attr) {
-            if (cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) != cudaSuccess)
-                return C2A_ERR_CUDA;
-            attr = true;
-        }
-        int *err = nullptr;
-        if (cudaGetSymbolAddress((void **)&err, g_tc_err) != cudaSuccess) return C2A_ERR_CUDA;
-        const dim3 grid(N / kTcN, M / kTcM);
-        k_gemm_tc<<<grid, kTcThreads, kTcSmem, (cudaStream_t)stream>>>(A, B, bias, M, N, K, flags, out_f32, out_bf16,
-                                                                       err);
-        return launch_status();
+    if (!attr) {
+        if (cudaFuncSetAttribute(k_gemm_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem) != cudaSuccess)
+            return C2A_ERR_CUDA;
+        attr = true;
     }
-    const dim3 grid(N / kBN, M / kBM);
-    k_gemm<<<grid, kGemmThreads, 0, (cudaStream_t)stream>>>(A, B, bias, M, N, K, flags, out_f32, out_bf16);
+    CUtensorMap ta, tb;
+    const cuuint64_t da[2] = {(cuuint64_t)K, (cuuint64_t)M}, db[2] = {(cuuint64_t)K, (cuuint64_t)N};
+    const cuuint64_t stride[1] = {(cuuint64_t)K * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcK, (cuuint32_t)kTcM}, es[2] = {1, 1};
+    if (encode(&ta, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)A, da, stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+            CUDA_SUCCESS ||
+        encode(&tb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)B, db, stride, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+            CUDA_SUCCESS)
+        return C2A_ERR_INVALID_ARGUMENT;
+    int *err = nullptr;
+    if (cudaGetSymbolAddress((void **)&err, g_tc_err) != cudaSuccess) return C2A_ERR_CUDA;
+    const dim3 grid(N / kTcN, M / kTcM);
+    k_gemm_tma<<<grid, kTcThreads, kTmSmem, (cudaStream_t)stream>>>(ta, tb, bias, M, N, K, flags, out_f32, out_bf16,
+                                                                     err);
     return launch_status();
 }
 
