@@ -50,7 +50,11 @@ def test_tuner_picks_a_measured_launch_and_caches_it(gpu_ctx, tmp_path, mode):
     rec = r["record"]
     names = [f"{tune.ENGINE_NAMES[e]}/{w or 'max'}" for e, w in t.candidates(wl.params)]
     assert sorted(rec["ms"]) == sorted(names) and not rec["cached"] and rec["sample_queries"] == 256
-    assert rec["choice"]["name"] == min(rec["ms"], key=rec["ms"].get)
+    exp, best = names[0], rec["ms"][names[0]]  # the default launch unless another is clearly faster
+    for nm in names[1:]:
+        if rec["ms"][nm] < best * (1 - rec["margin"]):
+            exp, best = nm, rec["ms"][nm]
+    assert rec["choice"]["name"] == exp
     assert r["params"]["engine"] == rec["choice"]["engine"]
     table = json.load(open(cache))
     assert list(table) == [rec["signature"]] and ("canonical" if mode else "reference") in rec["signature"]
