@@ -223,6 +223,10 @@ def implementation_dict(args, engine=None):
                          "node-pair test split across the lanes",
                  "thread": "reference order, one thread per query"}
     return {"engine": args.engine, "order": args.order if args.mode == "reference" else "geometric",
+            "learned_part": "the work-queue order: the seeding network trained as a cost model on measured query "
+                            "costs (64 log-cost buckets), queries taken costliest first; the seeding use of the "
+                            "network (CANONICAL hints) is measured by --mode learned"
+            if args.mode == "reference" and args.order == "learned" else None,
             "launch": "CUDA graph replay of the solve's launches (tune.GraphSolve)",
             "traversal": traversal.get(engine or ENGINE_OF.get(args.engine, args.engine), "canonical front")
             if args.mode == "reference" else
