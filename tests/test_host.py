@@ -139,3 +139,18 @@ def test_motion_matches_reference(lib):
         assert bits(c[:7]) == bits(z["consts"][i]), i
         R, T, qua = api.motion_integrate(z["R0"][i], z["T0"][i], z["R1"][i], z["T1"][i], z["t"][i])
         assert bits(R) == bits(z["Rt"][i]) and bits(T) == bits(z["Tt"][i]), i
+
+
+def test_fp64_probe_and_static_queries_validate_arguments(lib):
+    """Without a device the FP64 probe reports it; argument checks come first."""
+    import ctypes as C
+    from c2a_gb300 import api
+
+    f, a = C.c_double(), C.c_double()
+    assert lib.c2a_probe_fp64_peak(0, 1, C.byref(f), C.byref(a)) == api.ERR_NO_DEVICE
+    assert lib.c2a_probe_fp64_peak(0, 0, C.byref(f), C.byref(a)) == api.ERR_INVALID_ARGUMENT
+    assert lib.c2a_probe_fp64_peak(0, 1, None, C.byref(a)) == api.ERR_INVALID_ARGUMENT
+    with api.Context(-1) as ctx:
+        assert lib.c2a_collide_batch(ctx.h, None, 1, 3, 4, None, None) == api.ERR_INVALID_ARGUMENT  # flag 3
+        assert lib.c2a_tolerance_batch(ctx.h, None, 1, None, None) == api.ERR_INVALID_ARGUMENT
+        assert lib.c2a_tolerance_batch(ctx.h, None, 0, None, None) == api.ERR_NO_DEVICE
