@@ -462,7 +462,9 @@ c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias,
         ((flags & C2A_MLP_BIAS) && !bias) || ((uintptr_t)A & 15) || ((uintptr_t)B & 15))
         return C2A_ERR_INVALID_ARGUMENT;
     static PFN_encode_tiled encode = nullptr;
-    static bool attr = false;
+    static bool attr[128] = {}; /* the shared-memory opt-in is a per-device attribute */
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return C2A_ERR_CUDA;
     if (!encode) { /* the driver's tensor-map encoder, reached through the runtime */
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q;
@@ -472,10 +474,10 @@ c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias,
             return C2A_ERR_CUDA;
         encode = (PFN_encode_tiled)fn;
     }
-    if (!attr) {
+    if (!attr[dev]) {
         if (cudaFuncSetAttribute(k_gemm_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem) != cudaSuccess)
             return C2A_ERR_CUDA;
-        attr = true;
+        attr[dev] = true;
     }
     CUtensorMap ta, tb;
     const cuuint64_t da[2] = {(cuuint64_t)K, (cuuint64_t)M}, db[2] = {(cuuint64_t)K, (cuuint64_t)N};

@@ -167,12 +167,16 @@ class GraphSolve:
     """A batched solve captured once as a CUDA graph for fixed device buffers
     (queries, optional order, results, contacts) and replayed on whatever
     those buffers hold.  The first, uncaptured call sizes the library's
-    scratch so the captured launches allocate nothing."""
+    scratch so the captured launches allocate nothing.  The object keeps the
+    buffers alive for as long as the graph can be replayed; the context's
+    models must not change between replays (the graph holds the model table's
+    address)."""
 
     def __init__(self, ctx, d_queries, n: int, params: dict, d_results, d_contacts, contacts_per_query: int,
                  d_order=None, stream=None):
         torch = _torch()
         self.ctx, self.n = ctx, n
+        self._buffers = (d_queries, d_results, d_contacts, d_order)
         self.stream = stream or torch.cuda.Stream()
         ptrs = (d_queries.data_ptr(), d_results.data_ptr(), d_contacts.data_ptr() if d_contacts is not None else None)
 
