@@ -248,9 +248,12 @@ def run_learned(args, rank, world, local):
     if rank != 0:
         return
     t0 = time.time()
+    clocks = Clocks(local)
+    clocks.start()  # sampled over the whole experiment (labels, training and the timed batches)
     r = learned.experiment(n_train=args.train, n_eval=args.queries, epochs=args.epochs, pool=12,
                            tri_range=(1000, 200000), engine=api.ENGINE_BATCHED, seed=3,
                            log=lambda m: print(m, file=sys.stderr, flush=True))
+    clk = clocks.stop()
     ev, rp = r.pop("eval_workload"), r.pop("eval_results")
     # roofline of the hinted batch on the FP64 pipe: the reference counters' node-pair and triangle tests at the
     # per-unit flops of the REFERENCE path (the closest-pair search's node pairs are not in those counters, so
@@ -293,7 +296,7 @@ def run_learned(args, rank, world, local):
             "true_pair_hint_qps": args.queries / r["oracle_hint_ms"] * 1e3,
             "top1": r["top1"], "top8": r["topk"], "train_loss": r["loss"], "label_s": r["label_s"],
             "train_s": r["train_s"], "wall_s": time.time() - t0, "colliding": r["colliding"],
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": r["e2e_launches"]}
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "gpu_launches": r["e2e_launches"], "clocks": clk}
     print(json.dumps(line), flush=True)
 
 
