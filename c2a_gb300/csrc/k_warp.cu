@@ -82,3 +82,17 @@ __global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel
     }
 }
 
+
+#ifdef C2A_STATS
+/* profiling builds only: this translation unit's event counters, copied out and cleared */
+extern "C" int c2a_warp_stats_read(unsigned long long *out, int count)
+{
+    if (!out || count < ST_COUNT) return C2A_ERR_INVALID_ARGUMENT;
+    if (cudaDeviceSynchronize() != cudaSuccess) return C2A_ERR_CUDA;
+    if (cudaMemcpyFromSymbol(out, g_c2a_stats, sizeof(unsigned long long) * ST_COUNT) != cudaSuccess)
+        return C2A_ERR_CUDA;
+    unsigned long long zero[ST_COUNT] = {};
+    if (cudaMemcpyToSymbol(g_c2a_stats, zero, sizeof(zero)) != cudaSuccess) return C2A_ERR_CUDA;
+    return C2A_OK;
+}
+#endif
