@@ -32,6 +32,7 @@
 #include "ca_kernel.cuh"
 #include "rect_cases.cuh"
 #include "rect_table.cuh"
+#include "rect_table_ef.cuh"
 
 namespace c2a {
 
@@ -399,6 +400,66 @@ C2A_KDEV double rect_dist_half(const M3 &R, V3 T, const double a[2], const doubl
     return dt;
 }
 
+#if C2A_WARP_FILTER == 2
+/* rect_dist_half in the certified FP32 filter (rect_table_ef.cuh): the same
+ * slots, stages, comparison mask and operand tables with EF values; ok is
+ * false when a sort comparison, a case condition before the winner, the
+ * winner's own condition or its value could not be certified */
+C2A_KDEV EF rect_dist_half_e(const M3T<EF> &R, V3T<EF> T, const EF a[2], const EF b[2], V3T<EF> &S, EF *V, bool &ok,
+                             int lane)
+{
+    const int half = lane >> 4, k = lane & 15;
+    __syncwarp(); /* the previous call's reads of V are done */
+    rte_inputs(R, T, a, b, V);
+    __syncwarp();
+    if (k < kRtStage1) V[kRtInputs + k] = rte_stage1(k, R, T, V);
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const int i = k + 16 * r;
+        if (i < kRtStage2) V[kRtStage2Base + i] = rte_stage2(i, V);
+    }
+    __syncwarp();
+    const int cmp = k < 8 ? rte_compare(k, V) : 0;
+    const unsigned mask = (__ballot_sync(kWFull, cmp == 1) >> (16 * half)) & 0xffu;
+    const bool sort_bad = ((__ballot_sync(kWFull, cmp < 0) >> (16 * half)) & 0xffu) != 0u;
+    EF L[4], Rr[4], s1[7], s2[7], e[5], qb;
+    int px, py, qkind, cb, cu;
+    rte_case_operands(k, mask, V, L, Rr, s1, s2, e, qb, px, py, qkind, cb, cu);
+    EFCtx hc{false};
+    const bool holds = rte_case_holds(L, Rr, s1, s2, hc);
+    const unsigned m = (__ballot_sync(kWFull, holds && !hc.bad) >> (16 * half)) & 0xffffu;
+    const unsigned bad = (__ballot_sync(kWFull, hc.bad) >> (16 * half)) & 0xffffu;
+    const int win = m ? __ffs(m) - 1 : 16;
+    /* every case up to the winner (all sixteen when none holds) must be settled */
+    const unsigned upto = win < 16 ? ((1u << (win + 1)) - 1u) : 0xffffu;
+    ok = !sort_bad && (bad & upto) == 0u;
+    EF dj = ef_exact(0.0f);
+    V3T<EF> Sj = v3t(dj, dj, dj);
+    int vbad = 0;
+    if (m && k == win) {
+        EFCtx vc{false};
+        dj = rte_case_value(e, qb, px, py, qkind, cb, cu, R, T, a, Sj, vc);
+        vbad = vc.bad ? 1 : 0;
+    }
+    const int src = 16 * half + (win < 16 ? win : 0);
+    const EF dw = shfl_e(dj, src);
+    const V3T<EF> Sw = shfl_v3e(Sj, src);
+    const bool vb = __shfl_sync(kWFull, vbad, src) != 0;
+    if (m) {
+        S = Sw;
+        ok = ok && !vb;
+        return dw;
+    }
+    EFCtx tc{false};
+    V3T<EF> St = S;
+    const EF dt = rect_tail(R, T, a, b, St, tc);
+    S = St;
+    ok = ok && !tc.bad;
+    return dt;
+}
+#endif
+
 /* the children of an internal pair (C2A.cpp:1192-1226) */
 C2A_KDEV void split_pair(const Query &q, int b1, int b2, int fc1, int fc2, int &side, int &a1, int &a2, int &c1,
                          int &c2)
@@ -503,6 +564,18 @@ C2A_KDEV bool child_test_e(const Query &q, int x1, int x2, const M3 &R, V3 T, EF
     load_e(n1, q.A->snodes + x1);
     load_e(n2, q.B->snodes + x2);
     const EF zero = ef_exact(0.0f);
+#if C2A_WARP_FILTER == 2
+    C2A_WCLOCK(y0);
+    bool ok;
+    EF dist;
+    V3T<EF> S = v3t(zero, zero, zero);
+    {
+        bool rok = true;
+        dist = rect_dist_half_e(Re, Te, n1.l, n2.l, S, reinterpret_cast<EF *>(q.rt + 64 * half), rok, lane);
+        ok = rok && !pc.bad;
+        (void)j;
+    }
+#else
     V3T<EF> Sj = v3t(zero, zero, zero);
     int hit = 0;
     bool vbad = false;
@@ -528,6 +601,7 @@ C2A_KDEV bool child_test_e(const Query &q, int x1, int x2, const M3 &R, V3 T, EF
         S = St;
         ok = !tc.bad;
     }
+#endif
     C2A_WCLOCK(y1);
     C2A_WSTAT(q, ST_W_CYC_E_RECT, y1 - y0);
     const EF z = dist - (n1.r + n2.r);

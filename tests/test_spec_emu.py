@@ -18,12 +18,27 @@ WARP, SPEC = 1, 4
 SLOTS = 512
 
 
+def _build_emu(tmp_path_factory, name, defines=()):
+    out = str(tmp_path_factory.mktemp(name) / f"lib{name}.so")
+    subprocess.run(["g++", "-std=c++20", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
+                    "-w", *[f"-D{d}" for d in defines], "-o", out, os.path.join(ROOT, "tests", "cpp", "spec_emu.cpp"),
+                    os.path.join(ROOT, "c2a_gb300", "csrc", "host", "bvh_build.cpp")], check=True)
+    return out
+
+
+@pytest.fixture(scope="module")
+def emu_filter(tmp_path_factory):
+    """the warp engine with its node-pair tests in the certified FP32 filter
+    (the half-warp table form, C2A_WARP_FILTER=2)"""
+    lib = C.CDLL(_build_emu(tmp_path_factory, "emu_filter", ("C2A_WARP_FILTER=2",)))
+    lib.spec_emu_model.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    lib.spec_emu_solve.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+    return lib
+
+
 @pytest.fixture(scope="module")
 def emu(tmp_path_factory):
-    out = str(tmp_path_factory.mktemp("emu") / "libspec_emu.so")
-    subprocess.run(["g++", "-std=c++20", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
-                    "-w", "-o", out, os.path.join(ROOT, "tests", "cpp", "spec_emu.cpp"),
-                    os.path.join(ROOT, "c2a_gb300", "csrc", "host", "bvh_build.cpp")], check=True)
+    out = _build_emu(tmp_path_factory, "emu")
     lib = C.CDLL(out)
     lib.spec_emu_model.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
     lib.spec_emu_solve.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
@@ -77,3 +92,16 @@ def test_emulated_spec_matches_port_small_models(emu, port):
         offs = np.concatenate([[0], np.cumsum(np.minimum(SLOTS, pres["num_contact"]))])
         bad = result_mismatches(res, pres, con, flat, offs)
         assert not bad, describe(res, pres, bad[0])
+
+
+@pytest.mark.parametrize("name", ["config1", "mixed"])
+def test_emulated_filtered_warp_engine_matches_fixture(emu_filter, name):
+    """The filtered warp engine decides most node pairs from certified FP32
+    intervals and recomputes the rest in FP64: the reference's bits."""
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    sel = np.linspace(0, len(qint) - 1, 6).astype(int)
+    res, con = _run(emu_filter, ms, qint[sel], poses[sel], params, WARP)
+    flat = np.concatenate([econ[off[i]:off[i + 1]][:SLOTS] for i in sel])
+    offs = np.concatenate([[0], np.cumsum([min(SLOTS, off[i + 1] - off[i]) for i in sel])])
+    bad = result_mismatches(res, exp[sel], con, flat, offs)
+    assert not bad, describe(res, exp[sel], bad[0])
