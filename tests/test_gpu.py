@@ -263,3 +263,21 @@ def test_gpu_reference_engines_match_fixture(gpu_ctx, name, engine):
     assert (res["status"] == 0).all()
     bad = result_mismatches(res, exp, con, econ, off)
     assert not bad, f"engine {engine}: {len(bad)} of {len(exp)} differ; first " + describe(res, exp, bad[0])
+
+
+@pytest.mark.parametrize("engine", [0, 1, 3])
+def test_gpu_config2_1024_queries_every_field(gpu_ctx, port, engine):
+    """Config 2 (two 40,000-triangle knots, th_ca = 1e-4 diag): 1,024 queries
+    through the default, warp and thread engines, every result field (TOC
+    poses included) and every contact against the oracle."""
+    from c2a_gb300 import workloads
+
+    wl = workloads.config2(n=1024, seed=2, device="cpu")
+    res, con = gpu_solve(gpu_ctx, wl.meshes, wl.qint, wl.poses, dict(wl.params, engine=engine), slots=256)
+    pres, pcon = port.solve_batch(port.models(wl.meshes), wl.qint, wl.poses, wl.params, threads=os.cpu_count(),
+                                  contacts_per_query=256)
+    flat = np.concatenate([pcon[q][:min(256, pres[q]["num_contact"])] for q in range(wl.n)])
+    offs = np.concatenate([[0], np.cumsum(np.minimum(256, pres["num_contact"]))])
+    bad = result_mismatches(res, pres, con, flat, offs)
+    assert not bad, f"engine {engine}: {len(bad)} of {wl.n} differ; first " + describe(res, pres, bad[0])
+    assert 0.05 < 1 - res["collisionfree"].mean() < 0.95 and (res["status"] & ~4 == 0).all()
