@@ -52,6 +52,19 @@ __global__ void c2a_schedule_kernel(const c2a_query *__restrict__ queries, int n
 #ifndef C2A_WARP_MINB
 #define C2A_WARP_MINB 1
 #endif
+#ifdef C2A_QTIME
+/* profiling builds only: each query's start and end on the global timer (ns) */
+constexpr unsigned int kQtimeCap = 1u << 17;
+__device__ unsigned long long g_qtime[2 * kQtimeCap];
+extern "C" int c2a_warp_qtime_read(unsigned long long *out, int n)
+{
+    if (!out || n < 0 || (unsigned int)n > kQtimeCap) return C2A_ERR_INVALID_ARGUMENT;
+    if (cudaDeviceSynchronize() != cudaSuccess) return C2A_ERR_CUDA;
+    if (cudaMemcpyFromSymbol(out, g_qtime, sizeof(unsigned long long) * 2 * (size_t)n) != cudaSuccess)
+        return C2A_ERR_CUDA;
+    return C2A_OK;
+}
+#endif
 __global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel(const c2a_query *__restrict__ queries, int n,
                                                                   const DevModel *__restrict__ models,
                                                                   int num_models, c2a_params prm,
@@ -77,8 +90,20 @@ __global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel
             q = (unsigned int)o;
         }
         c2a_contact *cq = contacts ? contacts + (size_t)q * (size_t)prm.contacts_per_query : nullptr;
+#ifdef C2A_QTIME
+        unsigned long long t0;
+        asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t0));
+#endif
         solve_query_warp(queries[q], models, num_models, prm, results[q], cq, mine, tstack, (int)q, lane,
                          WarpDfs{mine});
+#ifdef C2A_QTIME
+        unsigned long long t1;
+        asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t1));
+        if (lane == 0 && q < kQtimeCap) {
+            g_qtime[2 * q] = t0;
+            g_qtime[2 * q + 1] = t1;
+        }
+#endif
     }
 }
 

@@ -48,7 +48,7 @@ def test_tuner_picks_a_measured_launch_and_caches_it(gpu_ctx, tmp_path, mode):
     t = tune.Tuner(gpu_ctx, cache=cache, sample=256, repeats=1)
     r = t.choose(d_q, wl.n, wl.params)
     rec = r["record"]
-    names = [f"{tune.ENGINE_NAMES[e]}/{w or 'max'}" for e, w in t.candidates(wl.params)]
+    names = [f"{tune.ENGINE_NAMES[e]}/{w or 'max'}" for e, w in t.candidates(wl.params) if not w]  # sample < batch
     assert sorted(rec["ms"]) == sorted(names) and not rec["cached"] and rec["sample_queries"] == 256
     exp, best = names[0], rec["ms"][names[0]]  # the default launch unless another is clearly faster
     for nm in names[1:]:
@@ -61,6 +61,9 @@ def test_tuner_picks_a_measured_launch_and_caches_it(gpu_ctx, tmp_path, mode):
     again = t.choose(d_q, wl.n, wl.params)
     assert again["record"]["cached"] and again["params"] == r["params"]
     # the tuned launch gives the default launch's results
+    # a sample that is the whole batch also times the launch shapes
+    whole = tune.Tuner(gpu_ctx, cache=None, sample=wl.n, repeats=1).measure(d_q, wl.n, wl.params)
+    assert sorted(whole["ms"]) == sorted(f"{tune.ENGINE_NAMES[e]}/{w or 'max'}" for e, w in t.candidates(wl.params))
     ref = _solve(gpu_ctx, d_q, wl.n, wl.params)
     got = _solve(gpu_ctx, d_q, wl.n, r["params"])
     assert ref[0].tobytes() == got[0].tobytes() and ref[1].tobytes() == got[1].tobytes()
