@@ -73,6 +73,8 @@ def parse():
                         "queries (costs measured by the library) starts the costliest queries first; geometric: "
                         "queries whose bounding spheres approach first.  Results are identical either way.")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--order-seeds", type=int, default=1,
+                   help="--order learned: batches of other seeds whose measured costs train the cost model")
     p.add_argument("--workload", choices=["config2", "config4"], default="config2",
                    help="config4: config 2 plus --near grazing near-contact queries (gap log-uniform [1e-6, 1e-3] "
                         "diag, velocity within 5 degrees of the tangent plane); reports the exact distance at "
@@ -370,15 +372,19 @@ def main():
 
         t_setup = time.time()
         diag = wl.meshes[0].bbox_diag()
-        wl_tr = workloads.config2(n=args.queries, seed=1000 + rank, device=f"cuda:{local}")
-        q_tr = wl_tr.qint.copy()
-        q_tr[:, :2] = mid
-        res_tr, _ = ctx.solve(q_tr, wl_tr.poses, wl.params, contacts_per_query=0)
-        cost_tr = learned.query_cost(res_tr)
-        f_tr = learned.features(wl_tr.poses, np.full(wl_tr.n, diag), np.full(wl_tr.n, diag))
-        cut = (wl_tr.n * 4 // 5) // 1024 * 1024  # 80 % to train on, the rest held out
+        costs, feats = [], []
+        for k in range(args.order_seeds):  # training batches of other seeds; their costs measured by the library
+            wl_tr = workloads.config2(n=args.queries, seed=1000 + 100 * k + rank, device=f"cuda:{local}")
+            q_tr = wl_tr.qint.copy()
+            q_tr[:, :2] = mid
+            res_tr, _ = ctx.solve(q_tr, wl_tr.poses, wl.params, contacts_per_query=0)
+            costs.append(learned.query_cost(res_tr))
+            feats.append(learned.features(wl_tr.poses, np.full(wl_tr.n, diag), np.full(wl_tr.n, diag)))
+        cost_tr, f_tr = np.concatenate(costs), np.concatenate(feats)
+        n_tr = len(cost_tr)
+        cut = (n_tr * 4 // 5) // 1024 * 1024  # 80 % to train on, the rest held out
         cost_model = learned.CostOrder(1, seed=rank)
-        zeros_tr = np.zeros(wl_tr.n, dtype=np.int32)
+        zeros_tr = np.zeros(n_tr, dtype=np.int32)
         epochs = max(30, -(-1536 // max(cut // 1024, 1)))  # about 1,500 optimizer steps whatever the batch size
         hist = cost_model.fit(f_tr[:cut], zeros_tr[:cut], zeros_tr[:cut], cost_tr[:cut], epochs=epochs)
         held = cost_model.expected(torch.tensor(f_tr[cut:], device="cuda"), torch.tensor(zeros_tr[cut:], device="cuda"),
@@ -386,7 +392,7 @@ def main():
         rank_r = float(np.corrcoef(np.argsort(np.argsort(held)), np.argsort(np.argsort(cost_tr[cut:])))[0, 1])
         feat_dev = torch.tensor(learned.features(wl.poses, np.full(n, diag), np.full(n, diag)), device="cuda")
         zeros_dev = torch.zeros(n, dtype=torch.int32, device="cuda")
-        learned_info = {"train_queries": cut, "held_out_queries": wl_tr.n - cut, "train_seed": 1000 + rank,
+        learned_info = {"train_queries": cut, "held_out_queries": n_tr - cut, "train_seeds": args.order_seeds,
                         "epochs": epochs, "final_loss": hist[-1], "held_out_rank_correlation": rank_r,
                         "used": rank_r >= 0.6, "setup_s": time.time() - t_setup}
 
