@@ -73,6 +73,9 @@ def parse():
                         "queries (costs measured by the library) starts the costliest queries first; geometric: "
                         "queries whose bounding spheres approach first.  Results are identical either way.")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--heavy", type=int, default=0,
+                   help="--order learned: the costliest queries at the head of the order that get an SM "
+                        "sub-partition of their own (c2a_params.heavy_prefix)")
     p.add_argument("--order-seeds", type=int, default=1,
                    help="--order learned: batches of other seeds whose measured costs train the cost model")
     p.add_argument("--workload", choices=["config2", "config4"], default="config2",
@@ -230,6 +233,7 @@ def implementation_dict(args, engine=None):
                             "network (CANONICAL hints) is measured by --mode learned"
             if args.mode == "reference" and args.order == "learned" else None,
             "launch": "CUDA graph replay of the solve's launches (tune.GraphSolve)",
+            "heavy_prefix": args.heavy if args.mode == "reference" and args.order == "learned" else 0,
             "traversal": traversal.get(engine or ENGINE_OF.get(args.engine, args.engine), "canonical front")
             if args.mode == "reference" else
             "canonical: each step seeded with the exact closest pair (the reference's C2A_Distance), order-free "
@@ -397,6 +401,8 @@ def main():
                         "used": rank_r >= 0.6, "setup_s": time.time() - t_setup}
 
         d_order = torch.arange(n, dtype=torch.int32, device="cuda")
+        if args.heavy and wl.params.get("engine", 0) in (ENGINES["auto"], ENGINES["warp"]):
+            wl.params["heavy_prefix"] = args.heavy
         ordered_graph = tune.GraphSolve(ctx, d_q, n, wl.params, d_r, d_c, CONTACT_SLOTS, d_order=d_order,
                                         stream=stream)
 

@@ -62,7 +62,7 @@ class Params(C.Structure):
     _fields_ = [("tol_d", C.c_double), ("tol_t", C.c_double), ("toc_delta", C.c_double),
                 ("contact_abs", C.c_double), ("with_contacts", C.c_int32), ("max_iters", C.c_int32),
                 ("qsize", C.c_int32), ("contacts_per_query", C.c_int32), ("mode", C.c_int32),
-                ("engine", C.c_int32), ("warps_per_sm", C.c_int32), ("reserved", C.c_int32)]
+                ("engine", C.c_int32), ("warps_per_sm", C.c_int32), ("heavy_prefix", C.c_int32)]
 
 
 MODE_REFERENCE, MODE_CANONICAL = 0, 1
@@ -163,7 +163,7 @@ def make_params(p: dict, contacts_per_query: int = 64) -> Params:
     return Params(float(p["tol_d"]), float(p["tol_t"]), float(p["toc_delta"]), float(p.get("contact_abs", 0.001)),
                   int(p.get("with_contacts", 1)), int(p.get("max_iters", 150)), int(p.get("qsize", 64)),
                   int(contacts_per_query), int(p.get("mode", MODE_REFERENCE)), int(p.get("engine", ENGINE_AUTO)),
-                  int(p.get("warps_per_sm", 0)), 0)
+                  int(p.get("warps_per_sm", 0)), int(p.get("heavy_prefix", 0)))
 
 
 def make_queries(qint: np.ndarray, poses: np.ndarray) -> np.ndarray:

@@ -96,6 +96,7 @@ struct c2a_context {
     size_t order_cap = 0;
     int canonical_blocks_per_sm = 0;
     int warp_blocks_per_sm = 0;
+    int split_smem_attr = 0;     /* the split warp kernel's dynamic shared-memory limit set so far */
     int warp_cap = 0;            /* the warp kernel's stack entries the occupancy above was computed for */
     bool warp_smem_attr = false;
     int distance_blocks_per_sm = 0;
@@ -178,7 +179,7 @@ c2a_status ensure_fronts(c2a_context *ctx, size_t warps, size_t want)
 
 bool params_ok(const c2a_params *p)
 {
-    return p && p->max_iters >= 0 && p->contacts_per_query >= 0 && p->warps_per_sm >= 0 && p->reserved == 0 &&
+    return p && p->max_iters >= 0 && p->contacts_per_query >= 0 && p->warps_per_sm >= 0 && p->heavy_prefix >= 0 &&
            (p->mode == C2A_MODE_REFERENCE || p->mode == C2A_MODE_CANONICAL) && p->engine >= C2A_ENGINE_AUTO &&
            p->engine <= C2A_ENGINE_SPEC && !(p->mode == C2A_MODE_REFERENCE && p->engine == C2A_ENGINE_BATCHED) &&
            !(p->mode == C2A_MODE_CANONICAL && (p->engine == C2A_ENGINE_THREAD || p->engine == C2A_ENGINE_SPEC));
@@ -670,6 +671,25 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
             C2A_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, c2a_solve_warp_kernel, kThreads, smem));
             ctx->warp_blocks_per_sm = occ > 0 ? occ : 1;
             ctx->warp_cap = cap;
+        }
+        const int heavy = prm.heavy_prefix < n ? prm.heavy_prefix : n;
+        if (user_order && heavy > 0) {
+            /* the head of the order on SM sub-partitions of its own (c2a_solve_warp_split_kernel) */
+            const size_t smem8 = warp_shared_bytes(cap) * (kSplitThreads / 32);
+            if ((int)smem8 > ctx->split_smem_attr) {
+                C2A_CUDA(cudaFuncSetAttribute(c2a_solve_warp_split_kernel,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem8));
+                ctx->split_smem_attr = (int)smem8;
+            }
+            int hb = (heavy + 3) / 4; /* four heavy warps per block */
+            if (hb > ctx->sm_count / 2) hb = ctx->sm_count / 2; /* at least half the SMs at full occupancy */
+            C2A_CUDA(cudaMemsetAsync(ctx->d_counter + 3, 0, sizeof(unsigned int), s));
+            c2a_solve_warp_split_kernel<<<ctx->sm_count, kSplitThreads, smem8, s>>>(
+                d_queries, n, heavy, hb, ctx->d_models, (int)ctx->models.size(), prm, d_results, d_contacts,
+                ctx->d_counter, ctx->d_counter + 3, user_order, cap);
+            ctx->launches++;
+            C2A_CUDA(cudaGetLastError());
+            return C2A_OK;
         }
         const int most = ctx->sm_count * blocks_per_sm(ctx->warp_blocks_per_sm, prm.warps_per_sm, kThreads);
         const int need = (int)(((int64_t)n * 32 + kThreads - 1) / kThreads);

@@ -108,6 +108,71 @@ __global__ void __launch_bounds__(kThreads, C2A_WARP_MINB) c2a_solve_warp_kernel
 }
 
 
+/* The same traversal for an ordered batch whose head holds its costliest
+ * queries.  One block of eight warps per SM (the register file holds one),
+ * warp w and warp w + 4 sharing an SM sub-partition.  In the first
+ * heavy_blocks blocks, warps 0..3 take the head's queries (order[0 ..
+ * n_heavy)) while their sub-partition mates wait, so a heavy query has its
+ * sub-partition's FP64 pipe to itself; a mate joins once the head is handed
+ * out and its partner is done.  Every other warp takes the rest of the order
+ * at full occupancy from the start.  The wait polls with a back-off and is
+ * bounded (it only affects speed). */
+__global__ void __launch_bounds__(kSplitThreads, 1) c2a_solve_warp_split_kernel(
+    const c2a_query *__restrict__ queries, int n, int n_heavy, int heavy_blocks, const DevModel *__restrict__ models,
+    int num_models, c2a_params prm, c2a_result *__restrict__ results, c2a_contact *__restrict__ contacts,
+    unsigned int *__restrict__ counter, unsigned int *__restrict__ heavy_counter, const int32_t *__restrict__ order,
+    int stack_cap)
+{
+    extern __shared__ __align__(16) unsigned char c2a_warp_smem[];
+    __shared__ volatile int busy[4];
+    Pending tstack[C2A_STACK_DEPTH];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    WarpShared &mine = *reinterpret_cast<WarpShared *>(c2a_warp_smem + warp * warp_shared_bytes(stack_cap));
+    mine.cap = stack_cap;
+    if (threadIdx.x < 4) busy[threadIdx.x] = 0;
+    __syncthreads();
+    const bool heavy_block = (int)blockIdx.x < heavy_blocks;
+    if (heavy_block && warp < 4) {
+        for (;;) {
+            unsigned int q = 0;
+            if (lane == 0) q = atomicAdd(heavy_counter, 1u);
+            q = __shfl_sync(kWFull, q, 0);
+            if (q >= (unsigned int)n_heavy) break;
+            const int32_t o = order[q];
+            if (o < 0 || o >= n) continue;
+            if (lane == 0) busy[warp] = 1;
+            __syncwarp();
+            c2a_contact *cq = contacts ? contacts + (size_t)o * (size_t)prm.contacts_per_query : nullptr;
+            solve_query_warp(queries[o], models, num_models, prm, results[o], cq, mine, tstack, o, lane,
+                             WarpDfs{mine});
+            __syncwarp();
+            if (lane == 0) busy[warp] = 0;
+        }
+    } else if (heavy_block) {
+        /* wait until the head is handed out and the partner's heavy query is done */
+        for (int it = 0; it < (1 << 24); it++) {
+            int done = 0;
+            if (lane == 0)
+                done = *reinterpret_cast<volatile unsigned int *>(heavy_counter) >= (unsigned int)n_heavy &&
+                       busy[warp - 4] == 0;
+            done = __shfl_sync(kWFull, done, 0);
+            if (done) break;
+            __nanosleep(2000);
+        }
+    }
+    for (;;) { /* the rest of the order */
+        unsigned int q = 0;
+        if (lane == 0) q = atomicAdd(counter, 1u);
+        q = __shfl_sync(kWFull, q, 0);
+        if (q >= (unsigned int)(n - n_heavy)) break;
+        const int32_t o = order[n_heavy + q];
+        if (o < 0 || o >= n) continue;
+        c2a_contact *cq = contacts ? contacts + (size_t)o * (size_t)prm.contacts_per_query : nullptr;
+        solve_query_warp(queries[o], models, num_models, prm, results[o], cq, mine, tstack, o, lane,
+                         WarpDfs{mine});
+    }
+}
+
 #ifdef C2A_STATS
 /* profiling builds only: this translation unit's event counters, copied out and cleared */
 extern "C" int c2a_warp_stats_read(unsigned long long *out, int count)

@@ -13,6 +13,7 @@
 
 namespace c2a {
 constexpr int kBlockThreads = 128; /* threads per block of the persistent solve kernels */
+constexpr int kSplitThreads = 256; /* the split warp kernel: eight warps, one block per SM */
 } // namespace c2a
 
 __global__ void c2a_solve_kernel(const c2a_query *__restrict__ queries, int n, const c2a::DevModel *__restrict__
@@ -41,6 +42,10 @@ __global__ void c2a_distance_kernel(const c2a_query *__restrict__ queries, int n
     models, int num_models, c2a_distance_result *__restrict__ results, unsigned int *__restrict__ counter,
     c2a::Pending *__restrict__ fronts);
 
+__global__ void c2a_solve_warp_split_kernel(const c2a_query *__restrict__ queries, int n, int n_heavy,
+    int heavy_blocks, const c2a::DevModel *__restrict__ models, int num_models, c2a_params prm,
+    c2a_result *__restrict__ results, c2a_contact *__restrict__ contacts, unsigned int *__restrict__ counter,
+    unsigned int *__restrict__ heavy_counter, const int32_t *__restrict__ order, int stack_cap);
 __global__ void c2a_tolerance_kernel(const c2a_query *__restrict__ queries, int n, const double *__restrict__ tolerance,
     const c2a::DevModel *__restrict__ models, int num_models, c2a_tolerance_result *__restrict__ results);
 __global__ void c2a_collide_kernel(const c2a_query *__restrict__ queries, int n, int flag,

@@ -83,7 +83,9 @@ typedef struct c2a_params {
     int32_t engine;             /* C2A_ENGINE_*; never changes a result */
     int32_t warps_per_sm;       /* launch shape: resident warps per SM of the solve kernel, 0 the most
                                    that fit (c2a_gb300.tune picks it); never changes a result */
-    int32_t reserved;           /* 0 */
+    int32_t heavy_prefix;       /* ordered REFERENCE batches on the warp engine: the first heavy_prefix
+                                   entries of the order (the costliest queries) each get an SM
+                                   sub-partition of their own; 0: none.  Never changes a result */
 } c2a_params;
 
 /* C2A_MODE_REFERENCE: the reference's results bit for bit (its depth-first

@@ -308,3 +308,38 @@ def test_gpu_order_desc_is_a_stable_counting_sort(gpu_ctx, n):
     assert lib.c2a_mlp_order_desc(d_k.data_ptr(), n, 63.0, d_o.data_ptr(), scratch.data_ptr(), None) == 0
     torch.cuda.synchronize()
     assert np.array_equal(d_o.cpu().numpy(), expect)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("heavy", [1, 24, 5000])
+def test_gpu_heavy_prefix_split_equals_plain(gpu_ctx, heavy):
+    """An ordered batch whose head runs on SM sub-partitions of its own
+    (c2a_params.heavy_prefix, the split warp kernel) gives the plain solve's
+    results and contacts bit for bit."""
+    import torch
+
+    wl = workloads.small_knots(400, seed=65)
+    mid = gpu_ctx.model(wl.meshes[0])
+    q = wl.qint.copy()
+    q[:, :2] = mid
+    plain, pc = gpu_ctx.solve(q, wl.poses, wl.params, contacts_per_query=64)
+    qs = api.make_queries(q, wl.poses)
+    n = len(qs)
+    d_q = torch.from_numpy(qs.view(np.uint8).copy()).cuda()
+    cost = plain["num_bv_tests"].astype(np.float64)
+    d_o = torch.tensor(np.argsort(-cost, kind="stable").astype(np.int32), device="cuda")
+    d_r = torch.zeros(n * api.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_c = torch.zeros(n * 64 * api.CONTACT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    launches = gpu_ctx.launches()
+    gpu_ctx.solve_ordered(d_q.data_ptr(), n, dict(wl.params, engine=api.ENGINE_WARP, heavy_prefix=heavy),
+                          d_o.data_ptr(), d_r.data_ptr(), d_c.data_ptr(), 64)
+    torch.cuda.synchronize()
+    assert gpu_ctx.launches() - launches == 1
+    r = d_r.cpu().numpy().view(api.RESULT_DTYPE)
+    c = d_c.cpu().numpy().view(api.CONTACT_DTYPE)
+    for f in RESULT_FIELDS:
+        assert bits(plain[f]) == bits(r[f]), f
+    for i in range(n):
+        m = min(int(plain[i]["num_contact"]), 64)
+        for f in ("tri_a", "tri_b", "distance", "pa", "pb"):
+            assert bits(pc[i][:m][f]) == bits(c[i * 64:i * 64 + m][f]), (i, f)
