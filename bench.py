@@ -76,7 +76,7 @@ def parse():
     p.add_argument("--heavy", type=int, default=0,
                    help="--order learned: the costliest queries at the head of the order that get an SM "
                         "sub-partition of their own (c2a_params.heavy_prefix)")
-    p.add_argument("--order-seeds", type=int, default=1,
+    p.add_argument("--order-seeds", type=int, default=3,
                    help="--order learned: batches of other seeds whose measured costs train the cost model")
     p.add_argument("--workload", choices=["config2", "config4"], default="config2",
                    help="config4: config 2 plus --near grazing near-contact queries (gap log-uniform [1e-6, 1e-3] "
