@@ -880,6 +880,11 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
 static_assert(sizeof(c2a_tolerance_result) == 80 && sizeof(c2a_collide_result) == 24, "record layouts");
 
 namespace {
+/* a pair per warp while the batch leaves every pair a warp slot (16 per SM),
+ * else a pair per lane: the lanes of a warp walk different trees, so packing
+ * pairs into a warp serialises their paths */
+int static_pairs_per_warp(const c2a_context *ctx, int n) { return n <= ctx->sm_count * 16 ? 1 : 32; }
+
 /* the host-buffer static queries: queries (and the per-query doubles) in,
  * one launch, results (and the pairs) out */
 c2a_status static_prepare(c2a_context *ctx, const c2a_query *queries, int32_t n)
@@ -911,8 +916,10 @@ c2a_status c2a_tolerance_batch(c2a_context *ctx, const c2a_query *queries, int32
         c2a_tolerance_result *dr = (c2a_tolerance_result *)(base + a + b);
         C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
         C2A_CUDA(cudaMemcpyAsync(dt, tolerance, sizeof(double) * nq, cudaMemcpyHostToDevice, ctx->stream));
-        c2a_tolerance_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
-            dq, n, dt, ctx->d_models, (int)ctx->models.size(), dr);
+        const int ppw = static_pairs_per_warp(ctx, n);
+        const int warps = (n + ppw - 1) / ppw;
+        c2a_tolerance_kernel<<<(warps * 32 + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
+            dq, n, dt, ctx->d_models, (int)ctx->models.size(), dr, ppw);
         ctx->launches++;
         C2A_CUDA(cudaGetLastError());
         C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_tolerance_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));
@@ -943,8 +950,10 @@ c2a_status c2a_collide_batch(c2a_context *ctx, const c2a_query *queries, int32_t
     c2a_collide_result *dr = (c2a_collide_result *)(base + a);
     int32_t *dp = slots ? (int32_t *)(base + a + r) : nullptr;
     C2A_CUDA(cudaMemcpyAsync(dq, queries, sizeof(c2a_query) * nq, cudaMemcpyHostToDevice, ctx->stream));
-    c2a_collide_kernel<<<(n + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
-        dq, n, flag, ctx->d_models, (int)ctx->models.size(), (int)slots, dr, dp);
+    const int ppw = static_pairs_per_warp(ctx, n);
+    const int warps = (n + ppw - 1) / ppw;
+    c2a_collide_kernel<<<(warps * 32 + kThreads - 1) / kThreads, kThreads, 0, ctx->stream>>>(
+        dq, n, flag, ctx->d_models, (int)ctx->models.size(), (int)slots, dr, dp, ppw);
     ctx->launches++;
     C2A_CUDA(cudaGetLastError());
     C2A_CUDA(cudaMemcpyAsync(results, dr, sizeof(c2a_collide_result) * nq, cudaMemcpyDeviceToHost, ctx->stream));

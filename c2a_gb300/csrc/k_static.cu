@@ -101,6 +101,17 @@ __device__ int static_obb_disjoint(const M3 &B, V3 Tv, const double *a, const do
     return 0;
 }
 
+/* the pair a thread owns: lane l of global warp w takes pair w * ppw + l when
+ * l < ppw (ppw 1: a pair per warp, for batches small enough to give every
+ * pair a warp; 32: a pair per lane), -1 otherwise */
+__device__ int static_pair_index(int ppw)
+{
+    const int lane = threadIdx.x & 31;
+    if (lane >= ppw) return -1;
+    const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    return warp * ppw + lane;
+}
+
 __device__ bool static_query_ok(const c2a_query &in, const DevModel *models, int num_models)
 {
     return in.model_a >= 0 && in.model_a < num_models && in.model_b >= 0 && in.model_b < num_models &&
@@ -112,10 +123,11 @@ __device__ bool static_query_ok(const c2a_query &in, const DevModel *models, int
 __global__ void __launch_bounds__(kBlockThreads) c2a_tolerance_kernel(const c2a_query *__restrict__ queries, int n,
                                                                  const double *__restrict__ tolerance,
                                                                  const DevModel *__restrict__ models, int num_models,
-                                                                 c2a_tolerance_result *__restrict__ results)
+                                                                 c2a_tolerance_result *__restrict__ results,
+                                                                 int pairs_per_warp)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = static_pair_index(pairs_per_warp);
+    if (i < 0 || i >= n) return;
     const c2a_query &in = queries[i];
     c2a_tolerance_result out;
     memset(&out, 0, sizeof(out));
@@ -203,10 +215,10 @@ __global__ void __launch_bounds__(kBlockThreads) c2a_tolerance_kernel(const c2a_
 __global__ void __launch_bounds__(kBlockThreads) c2a_collide_kernel(const c2a_query *__restrict__ queries, int n, int flag,
                                                                const DevModel *__restrict__ models, int num_models,
                                                                int slots, c2a_collide_result *__restrict__ results,
-                                                               int32_t *__restrict__ pairs)
+                                                               int32_t *__restrict__ pairs, int pairs_per_warp)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int i = static_pair_index(pairs_per_warp);
+    if (i < 0 || i >= n) return;
     const c2a_query &in = queries[i];
     c2a_collide_result out;
     memset(&out, 0, sizeof(out));

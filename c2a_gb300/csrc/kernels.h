@@ -47,9 +47,10 @@ __global__ void c2a_solve_warp_split_kernel(const c2a_query *__restrict__ querie
     c2a_result *__restrict__ results, c2a_contact *__restrict__ contacts, unsigned int *__restrict__ counter,
     unsigned int *__restrict__ heavy_counter, const int32_t *__restrict__ order, int stack_cap);
 __global__ void c2a_tolerance_kernel(const c2a_query *__restrict__ queries, int n, const double *__restrict__ tolerance,
-    const c2a::DevModel *__restrict__ models, int num_models, c2a_tolerance_result *__restrict__ results);
+    const c2a::DevModel *__restrict__ models, int num_models, c2a_tolerance_result *__restrict__ results,
+    int pairs_per_warp);
 __global__ void c2a_collide_kernel(const c2a_query *__restrict__ queries, int n, int flag,
     const c2a::DevModel *__restrict__ models, int num_models, int slots, c2a_collide_result *__restrict__ results,
-    int32_t *__restrict__ pairs);
+    int32_t *__restrict__ pairs, int pairs_per_warp);
 
 #endif
