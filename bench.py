@@ -10,11 +10,21 @@ t_delta = 1e-4, contacts within 2 d + 0.001 enumerated at every TOC, the
 reference's traversal order and seeds (triangle 0 of each model).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config2|config4] [--mode reference|canonical|learned]
 
-value: queries/s with the queries already in HBM (device entry point,
-CUDA events around the kernel on its stream, L2 flushed between steps).
-e2e: the same through c2a_solve_batch with host buffers (H2D of the queries,
-D2H of results and dense contacts inside the timed region).
+Before timing: the autotuner picks the launch on a strided sample of the
+batch, and a cost model (the seeding network trained on other batches'
+measured query costs) orders the batch costliest first.  Each timed step is
+the network's inference, the library's ordering kernels and a CUDA-graph
+replay of the ordered solve.
+value: queries/s with the queries already in HBM (CUDA events on the
+launching stream, L2 flushed between steps).
+e2e: the same pipeline from host buffers (pose features computed on the host,
+queries H2D, results and dense contacts D2H inside the timed region).
+roofline: the algorithm's FP64 flops per launch (per-unit counts from the
+oracle's own arithmetic) against the FP64 peak measured in the same run.
+cpu_baseline: the oracle port on all host cores over a strided sample,
+compared with the GPU's results field by field and contact by contact.
 --impl reference: the CPU oracle port of the reference (bit-identical to
 the reference's own code) on all host cores, on a bounded sample.
 Under torchrun each rank runs its own replica batch (queries are independent).
