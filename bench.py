@@ -266,8 +266,9 @@ def run_learned(args, rank, world, local):
     t0 = time.time()
     clocks = Clocks(local)
     clocks.start()  # sampled over the whole experiment (labels, training and the timed batches)
+    engine = api.ENGINE_WARP if args.engine == "warp" else api.ENGINE_BATCHED  # auto: the batched engine
     r = learned.experiment(n_train=args.train, n_eval=args.queries, epochs=args.epochs, pool=12,
-                           tri_range=(1000, 200000), engine=api.ENGINE_BATCHED, seed=3,
+                           tri_range=(1000, 200000), engine=engine, seed=3,
                            log=lambda m: print(m, file=sys.stderr, flush=True))
     clk = clocks.stop()
     ev, rp = r.pop("eval_workload"), r.pop("eval_results")
@@ -279,7 +280,8 @@ def run_learned(args, rank, world, local):
     achieved = (bv * F_BV + tri * F_TRI) / (r["hinted_ms"] / 1e3) / 1e9
     roofline = {"bound": "fp64", "achieved": achieved, "peak": fma_peak / 1e9, "unit": "GFLOP/s",
                 "frac": achieved / (fma_peak / 1e9), "traffic": None, "peak_unfused": add_peak / 1e9,
-                "peak_source": "measured in this run: c2a_probe_fp64_peak", "kernel": "k_dsearch + step waves",
+                "peak_source": "measured in this run: c2a_probe_fp64_peak",
+                "kernel": "c2a_canonical_kernel" if engine == api.ENGINE_WARP else "k_dsearch + step waves",
                 "note": "counts only the step's node-pair and triangle tests (num_bv_tests, num_tri_tests); the "
                         "closest-pair search that seeds every step is not in those counters"}
     cpu = None
@@ -305,7 +307,8 @@ def run_learned(args, rank, world, local):
             "data": "synthetic: seeded config-3 mesh pool (torus knots, noisy icospheres, clustered soups)",
             "config": {"workload": f"config3 pool of 12 meshes ({min(r['pool_tris'])}-{max(r['pool_tris'])} "
                                    f"triangles), {args.queries} held-out queries", "mode": "canonical",
-                       "engine": "batched", "train_queries": args.train, "epochs": args.epochs,
+                       "engine": "warp" if engine == api.ENGINE_WARP else "batched", "train_queries": args.train,
+                       "epochs": args.epochs,
                        "network": "50->256->256->256->4096, GELU, bf16 weights, fp32 accumulation", "top_k": 8},
             "plain_qps": r["plain_qps"], "speedup_vs_plain": r["speedup"], "identical_results": r["identical"],
             "differing_fields": r["differ"], "contact_overflow_queries": r["contact_overflow_queries"],
