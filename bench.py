@@ -242,7 +242,8 @@ def implementation_dict(args, engine=None):
                             "costs (64 log-cost buckets), queries taken costliest first; the seeding use of the "
                             "network (CANONICAL hints) is measured by --mode learned"
             if args.mode == "reference" and args.order == "learned" else None,
-            "launch": "CUDA graph replay of the solve's launches (tune.GraphSolve)",
+            "launch": "CUDA graph replay of each step (tune.GraphSolve): with the learned order, the network's "
+                      "inference, the ordering kernels and the ordered solve in one graph",
             "heavy_prefix": args.heavy if args.mode == "reference" and args.order == "learned" else 0,
             "traversal": traversal.get(engine or ENGINE_OF.get(args.engine, args.engine), "canonical front")
             if args.mode == "reference" else
@@ -416,12 +417,13 @@ def main():
         d_order = torch.arange(n, dtype=torch.int32, device="cuda")
         if args.heavy and wl.params.get("engine", 0) in (ENGINES["auto"], ENGINES["warp"]):
             wl.params["heavy_prefix"] = args.heavy
+        # one CUDA graph per step: the network's inference, the ordering kernels and the ordered solve
         ordered_graph = tune.GraphSolve(ctx, d_q, n, wl.params, d_r, d_c, CONTACT_SLOTS, d_order=d_order,
-                                        stream=stream)
+                                        stream=stream,
+                                        prologue=lambda: d_order.copy_(cost_model.order(feat_dev, zeros_dev,
+                                                                                        zeros_dev)))
 
         def learned_step():
-            with torch.cuda.stream(stream):
-                d_order.copy_(cost_model.order(feat_dev, zeros_dev, zeros_dev))
             ordered_graph.replay()
 
         if learned_info["used"]:  # a model that does not rank held-out costs leaves the geometric order

@@ -176,13 +176,15 @@ class GraphSolve:
     """A batched solve captured once as a CUDA graph for fixed device buffers
     (queries, optional order, results, contacts) and replayed on whatever
     those buffers hold.  The first, uncaptured call sizes the library's
-    scratch so the captured launches allocate nothing.  The object keeps the
+    scratch so the captured launches allocate nothing.  An optional prologue
+    (a callable issuing device work on the current stream, such as the
+    network that writes the order) is captured ahead of the solve.  The object keeps the
     buffers alive for as long as the graph can be replayed; the context's
     models must not change between replays (the graph holds the model table's
     address)."""
 
     def __init__(self, ctx, d_queries, n: int, params: dict, d_results, d_contacts, contacts_per_query: int,
-                 d_order=None, stream=None):
+                 d_order=None, stream=None, prologue=None):
         torch = _torch()
         self.ctx, self.n = ctx, n
         self._buffers = (d_queries, d_results, d_contacts, d_order)
@@ -190,6 +192,9 @@ class GraphSolve:
         ptrs = (d_queries.data_ptr(), d_results.data_ptr(), d_contacts.data_ptr() if d_contacts is not None else None)
 
         def call(stream_handle):
+            if prologue is not None:  # device work that prepares the buffers (e.g. the order), on the same stream
+                with torch.cuda.stream(self.stream):
+                    prologue()
             if d_order is None:
                 ctx.solve_device(ptrs[0], n, params, ptrs[1], ptrs[2], contacts_per_query, stream=stream_handle)
             else:

@@ -99,3 +99,28 @@ def test_graph_replay_matches_direct_solves(gpu_ctx, engine):
         assert d_c.cpu().numpy().tobytes() == exp[1].tobytes()
     r = d_r.cpu().numpy().view(api.RESULT_DTYPE)
     assert (r["status"] & ~api.QUERY_CONTACT_OVERFLOW == 0).all() and bits(r["toc"]) != bits(np.zeros(n))
+
+
+def test_graph_with_prologue_captures_the_order(gpu_ctx):
+    """A prologue captured ahead of the solve (here: the order written on the
+    device) is replayed with it."""
+    import torch
+    from c2a_gb300 import api, tune
+
+    n, slots = 256, 64
+    wl, q, d_q = _batch(gpu_ctx, n, 84)
+    prm = dict(wl.params, engine=api.ENGINE_WARP)
+    perm = torch.tensor(np.random.default_rng(85).permutation(n).astype(np.int32), device="cuda")
+    d_order = torch.zeros(n, dtype=torch.int32, device="cuda")
+    d_r = torch.zeros(n * api.RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    d_c = torch.zeros(n * slots * api.CONTACT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    g = tune.GraphSolve(gpu_ctx, d_q, n, prm, d_r, d_c, slots, d_order=d_order,
+                        prologue=lambda: d_order.copy_(torch.flip(perm, dims=[0])))
+    d_order.zero_()
+    d_r.zero_()
+    torch.cuda.synchronize()
+    g.replay()
+    g.stream.synchronize()
+    assert torch.equal(d_order, torch.flip(perm, dims=[0]))
+    exp = _solve(gpu_ctx, d_q, n, prm, slots)
+    assert d_r.cpu().numpy().tobytes() == exp[0].tobytes()
