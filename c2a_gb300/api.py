@@ -47,7 +47,7 @@ NOALLOC_MAX_MODELS = 120  # C2A_NOALLOC_MAX_MODELS
 
 # every extern "C" symbol of include/c2a_gb300.h
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
-               "c2a_model_info", "c2a_model_download", "c2a_model_download_obb", "c2a_model_free",
+               "c2a_model_build_many", "c2a_model_info", "c2a_model_download", "c2a_model_download_obb", "c2a_model_free",
                "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
                "c2a_distance_batch", "c2a_solve_batch_hinted", "c2a_solve_batch_ordered",
@@ -116,6 +116,7 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_status_str": ([i32], C.c_char_p),
         "c2a_launch_count": ([vp, C.POINTER(C.c_int64)], i32),
         "c2a_model_build": ([vp, i32, vp, vp, vp, C.POINTER(i32)], i32),
+        "c2a_model_build_many": ([vp, i32, vp, vp, vp, vp, i32, vp], i32),
         "c2a_model_info": ([vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
         "c2a_model_download": ([vp, i32, vp, vp, vp, vp, vp], i32),
         "c2a_model_download_obb": ([vp, i32, vp], i32),
@@ -230,8 +231,22 @@ class Context:
                "c2a_model_build")
         return mid.value
 
-    def models(self, meshes) -> list:
-        return [self.model(m) for m in meshes]
+    def models(self, meshes, threads: int = 0) -> list:
+        """Builds every mesh at once on parallel host threads (c2a_model_build_many); ids in the order given."""
+        meshes = list(meshes)
+        if not meshes:
+            return []
+        tvs = [mesh.tri_verts() for mesh in meshes]
+        vidxs = [np.ascontiguousarray(mesh.faces, dtype=np.int32) for mesh in meshes]
+        n = len(meshes)
+        counts = np.array([mesh.num_tris for mesh in meshes], dtype=np.int32)
+        tv_ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in tvs])
+        vidx_ptrs = (C.c_void_p * n)(*[a.ctypes.data for a in vidxs])
+        ids = np.full(n, -1, dtype=np.int32)
+        _check(self.lib.c2a_model_build_many(self.h, n, _ptr(counts), C.cast(tv_ptrs, C.c_void_p), None,
+                                             C.cast(vidx_ptrs, C.c_void_p), int(threads), _ptr(ids)),
+               "c2a_model_build_many")
+        return [int(i) for i in ids]
 
     def model_info(self, mid: int) -> tuple[int, int, int]:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()

@@ -6,11 +6,15 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <atomic>
 #include <mutex>
 #include <new>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/c2a_gb300.h"
@@ -404,14 +408,23 @@ c2a_status c2a_launch_count(c2a_context *ctx, int64_t *count)
     return C2A_OK;
 }
 
-c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
-                           const int32_t *vidx, int32_t *model_id)
+namespace {
+
+/* host threads a build may use: C2A_BUILD_THREADS when set (>= 1), else every hardware thread */
+int build_thread_count(int32_t requested)
 {
-    if (!ctx || !model_id) return C2A_ERR_INVALID_ARGUMENT;
-    ModelSlot slot;
-    int rc = build_rss_model(num_tris, tri_verts, ids, vidx, slot.host);
-    if (rc) return rc;
-    std::lock_guard<std::mutex> lock(ctx->mu);
+    if (requested > 0) return requested;
+    if (const char *e = getenv("C2A_BUILD_THREADS")) {
+        const int v = atoi(e);
+        if (v > 0) return v;
+    }
+    const unsigned h = std::thread::hardware_concurrency();
+    return h ? (int)h : 1;
+}
+
+/* uploads a built model and adds it to the context's table (ctx->mu held) */
+c2a_status register_model(c2a_context *ctx, ModelSlot &slot, int32_t *model_id)
+{
     if (ctx->device < 0) {
         slot.live = true;
         ctx->models.push_back(std::move(slot));
@@ -452,6 +465,80 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
     ctx->models_dirty = true;
     ctx->models_gen = next_models_gen();
     *model_id = (int32_t)ctx->models.size() - 1;
+    return C2A_OK;
+}
+
+} // namespace
+
+c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
+                           const int32_t *vidx, int32_t *model_id)
+{
+    if (!ctx || !model_id) return C2A_ERR_INVALID_ARGUMENT;
+    ModelSlot slot;
+    BuildThreads threads(build_thread_count(0) - 1);
+    int rc = build_rss_model(num_tris, tri_verts, ids, vidx, slot.host, &threads);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    return register_model(ctx, slot, model_id);
+}
+
+c2a_status c2a_model_build_many(c2a_context *ctx, int32_t count, const int32_t *num_tris,
+                                const double *const *tri_verts, const int32_t *const *ids,
+                                const int32_t *const *vidx, int32_t threads, int32_t *model_ids)
+{
+    if (!ctx || count < 0 || (count > 0 && (!num_tris || !tri_verts || !model_ids)) || threads < 0)
+        return C2A_ERR_INVALID_ARGUMENT;
+    for (int32_t i = 0; i < count; i++)
+        if (num_tris[i] <= 0 || !tri_verts[i]) return C2A_ERR_EMPTY_MODEL;
+    if (count == 0) return C2A_OK;
+    // largest models first; one worker per model at a time, and a worker
+    // with no model left lends its thread to the builds still running
+    std::vector<int32_t> order((size_t)count);
+    for (int32_t i = 0; i < count; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return num_tris[a] > num_tris[b]; });
+    std::vector<ModelSlot> slots((size_t)count);
+    std::vector<int> rcs((size_t)count, 0);
+    const int total = build_thread_count(threads);
+    const int workers = std::min(total, (int)count);
+    BuildThreads budget(total - workers);
+    std::atomic<int32_t> next{0};
+    auto work = [&] {
+        for (int32_t k; (k = next.fetch_add(1)) < count;) {
+            const int32_t i = order[k];
+            rcs[i] = build_rss_model(num_tris[i], tri_verts[i], ids ? ids[i] : nullptr, vidx ? vidx[i] : nullptr,
+                                     slots[i].host, &budget);
+        }
+        budget.give();
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < workers; w++) {
+        try {
+            pool.emplace_back(work);
+        } catch (const std::system_error &) {
+            break; // fewer workers; the ones running take the rest
+        }
+    }
+    work();
+    for (std::thread &th : pool) th.join();
+    for (int32_t i = 0; i < count; i++)
+        if (rcs[i]) return rcs[i];
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    for (int32_t i = 0; i < count; i++) {
+        const c2a_status s = register_model(ctx, slots[i], &model_ids[i]);
+        if (s != C2A_OK) {
+            for (int32_t j = 0; j < i; j++) {
+                ModelSlot &done = ctx->models[model_ids[j]];
+                if (ctx->device >= 0) free_slot(done);
+                done.live = false;
+                done.host = BuiltModel{};
+                model_ids[j] = -1;
+            }
+            model_ids[i] = -1;
+            ctx->models_dirty = true;
+            ctx->models_gen = next_models_gen();
+            return s;
+        }
+    }
     return C2A_OK;
 }
 

@@ -13,15 +13,25 @@
  * fitted, the left subtree is built before the right one), so node and
  * triangle indices match the reference's.
  *
+ * Subtrees build on parallel host threads when a BuildThreads budget is
+ * given.  Every node's fit, sums and partition still run in the reference's
+ * order on one thread, and a subtree of k triangles always holds 2k - 1
+ * nodes, so each node's number follows from its parent's number and the
+ * left part's size alone: the tree is the same bits whatever the threads.
+ *
  * PQP's eigen-solver is not part of the reference; the Jacobi sweep below is
  * the one the CPU oracle uses, so both build the same tree.  Compile with
  * -ffp-contract=off.
  */
 #include "bvh_build.h"
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <new>
+#include <stdexcept>
+#include <thread>
 
 #include "../../../include/c2a_gb300.h"
 
@@ -68,34 +78,67 @@ struct AbsNode {
     int32_t depth;
 };
 
+/* one node still to fit: its triangles tris[first, first+count), and base,
+ * the number its first child gets (the reference's allocation counter when
+ * this node is fitted) */
+struct BuildTask {
+    int32_t node, first, count, parent, depth, base;
+};
+
+/* subtrees smaller than this stay on the thread that split them */
+constexpr int32_t kSpawnGrain = 4096;
+
 class Builder {
   public:
-    Builder(std::vector<Tri> &tris, std::vector<AbsNode> &nodes) : tris_(tris), nodes_(nodes) {}
-
-    void run()
+    Builder(RecordVec<Tri> &tris, RecordVec<AbsNode> &nodes, BuildThreads *threads)
+        : tris_(tris), nodes_(nodes), threads_(threads)
     {
-        const int32_t n = (int32_t)tris_.size();
-        proj_.resize(9 * (size_t)n);
-        next_free_ = 1;
-        struct Item {
-            int32_t node, first, count, parent, depth;
-        };
-        std::vector<Item> stack;
-        stack.push_back({0, 0, n, -1, 0});
-        while (!stack.empty()) {
-            Item it = stack.back();
-            stack.pop_back();
-            int32_t nfirst = fit_and_split(it.node, it.first, it.count);
-            AbsNode &b = nodes_[it.node];
-            b.parent = it.parent;
-            b.depth = it.depth;
-            if (it.count > 1) {
-                // right pushed first so the left subtree is built (and numbered) first
-                stack.push_back({b.first_child + 1, it.first + nfirst, it.count - nfirst, it.node, it.depth + 1});
-                stack.push_back({b.first_child, it.first, nfirst, it.node, it.depth + 1});
-            }
-        }
     }
+
+    void run() { build_from({0, 0, (int32_t)tris_.size(), -1, 0, 1}, false); }
+
+  private:
+    /* builds the subtree of task t depth first, left before right; a right
+     * subtree of at least kSpawnGrain triangles goes to a new thread when the
+     * budget has one to spare.  holds_thread: this call runs on a thread
+     * taken from the budget, given back once its own work is done. */
+    void build_from(BuildTask t0, bool holds_thread)
+    {
+        std::vector<std::thread> spawned;
+        try {
+            std::vector<double> proj;
+            std::vector<BuildTask> stack;
+            stack.push_back(t0);
+            while (!stack.empty()) {
+                const BuildTask t = stack.back();
+                stack.pop_back();
+                const int32_t nleft = fit_and_split(t, proj);
+                if (t.count == 1) continue;
+                // a subtree of k triangles allocates 2k - 2 nodes below its root
+                const BuildTask left{t.base, t.first, nleft, t.node, t.depth + 1, t.base + 2};
+                const BuildTask right{t.base + 1, t.first + nleft, t.count - nleft, t.node, t.depth + 1,
+                                      t.base + 2 * nleft};
+                bool handed_off = false;
+                if (threads_ && right.count >= kSpawnGrain && threads_->take()) {
+                    try {
+                        spawned.emplace_back([this, right] { build_from(right, true); });
+                        handed_off = true;
+                    } catch (const std::exception &) { // no thread (system_error) or no room to keep it
+                        threads_->give();
+                    }
+                }
+                if (!handed_off) stack.push_back(right);
+                stack.push_back(left);
+            }
+        } catch (const std::bad_alloc &) {
+            failed_ = true;
+        }
+        if (holds_thread) threads_->give();
+        for (std::thread &th : spawned) th.join();
+    }
+
+  public:
+    bool failed() const { return failed_; }
 
   private:
     // covariance of the vertices of tris[first, first+n)
@@ -125,7 +168,7 @@ class Builder {
     }
 
     // RSS fit of tris[first, first+n) in frame R (FitToTris_Corner, RSS part)
-    void fit(AbsNode &b, const double R[3][3], int32_t first, int32_t n)
+    void fit(AbsNode &b, const double R[3][3], int32_t first, int32_t n, std::vector<double> &proj)
     {
         b.angR = 0.0;
         for (int32_t i = first; i < first + n; i++)
@@ -136,7 +179,8 @@ class Builder {
             }
         std::memcpy(b.R, R, sizeof(b.R));
         const int32_t np = 3 * n;
-        double *P = proj_.data();
+        if (proj.size() < 9 * (size_t)n) proj.resize(9 * (size_t)n);
+        double *P = proj.data();
         for (int32_t i = 0; i < n; i++)
             for (int k = 0; k < 3; k++) rt_mul(P + 9 * i + 3 * k, b.R, tris_[first + i].p[k]);
         auto X = [P](int32_t k) { return P[3 * k]; };
@@ -253,10 +297,12 @@ class Builder {
         if (b.l[1] < 0) b.l[1] = 0;
     }
 
-    // fits node bn to tris[first, first+n); for n > 1 allocates its children
-    // and partitions the range; returns the size of the left part
-    int32_t fit_and_split(int32_t bn, int32_t first, int32_t n)
+    // fits node t.node to its triangles; for more than one numbers its
+    // children t.base, t.base + 1 and partitions the range; returns the size
+    // of the left part
+    int32_t fit_and_split(const BuildTask &t, std::vector<double> &proj)
     {
+        const int32_t first = t.first, n = t.count;
         double C[3][3], E[3][3], s[3], R[3][3];
         covariance(C, first, n);
         jacobi_eigen3(E, s, C);
@@ -285,14 +331,15 @@ class Builder {
         R[1][2] = E[0][mid] * E[2][mx] - E[0][mx] * E[2][mid];
         R[2][2] = E[0][mx] * E[1][mid] - E[0][mid] * E[1][mx];
 
-        AbsNode &b = nodes_[bn];
-        fit(b, R, first, n);
+        AbsNode &b = nodes_[t.node];
+        b.parent = t.parent;
+        b.depth = t.depth;
+        fit(b, R, first, n, proj);
         if (n == 1) {
             b.first_child = -(first + 1);
             return 1;
         }
-        b.first_child = next_free_;
-        next_free_ += 2;
+        b.first_child = t.base;
 
         // split at the mean vertex along the major axis; centroids <= mean go left
         const double axis[3] = {R[0][0], R[1][0], R[2][0]};
@@ -321,10 +368,10 @@ class Builder {
         return left;
     }
 
-    std::vector<Tri> &tris_;
-    std::vector<AbsNode> &nodes_;
-    std::vector<double> proj_;
-    int32_t next_free_ = 1;
+    RecordVec<Tri> &tris_;
+    RecordVec<AbsNode> &nodes_;
+    BuildThreads *threads_;
+    std::atomic<bool> failed_{false}; /* a thread ran out of memory */
 };
 
 } // namespace
@@ -382,78 +429,158 @@ float shadow_of(double x, bool &ok)
 }
 } // namespace
 
-int build_rss_model(int32_t num_tris, const double *tv, const int32_t *ids, const int32_t *vidx, BuiltModel &out)
+bool BuildThreads::take()
 {
-    if (num_tris <= 0 || !tv) return C2A_ERR_EMPTY_MODEL;
-    std::vector<Tri> tris((size_t)num_tris);
-    for (int32_t i = 0; i < num_tris; i++) {
-        std::memcpy(tris[i].p, tv + 9 * (size_t)i, sizeof(tris[i].p));
-        tris[i].id = ids ? ids[i] : i;
-        for (int k = 0; k < 3; k++) tris[i].idx[k] = vidx ? vidx[3 * (size_t)i + k] : -1;
-    }
-    const int32_t num_nodes = 2 * num_tris - 1;
-    std::vector<AbsNode> nodes((size_t)num_nodes);
-    Builder(tris, nodes).run();
+    int f = free_.load(std::memory_order_relaxed);
+    while (f > 0)
+        if (free_.compare_exchange_weak(f, f - 1, std::memory_order_acq_rel)) return true;
+    return false;
+}
 
-    out.nodes.assign((size_t)num_nodes, NodeRec{});
-    out.obbs.assign((size_t)num_nodes, ObbRec{});
-    out.tris.assign((size_t)num_tris, TriRec{});
-    out.depth = 0;
-    for (int32_t i = 0; i < num_nodes; i++) {
-        const AbsNode &b = nodes[i];
-        NodeRec &o = out.nodes[i];
-        // parent-relative frame: R = Rp^T R, Tr = Rp^T (Tr - Trp); the root is
-        // taken relative to the identity exactly as the reference does
-        static const double I[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
-        static const double Z[3] = {0.0, 0.0, 0.0};
-        const double(*PR)[3] = b.parent >= 0 ? nodes[b.parent].R : I;
-        const double *PT = b.parent >= 0 ? nodes[b.parent].Tr : Z;
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++) {
-                o.R[3 * r + c] = PR[0][r] * b.R[0][c] + PR[1][r] * b.R[1][c] + PR[2][r] * b.R[2][c];
-                o.Rloc[3 * r + c] = b.R[r][c];
-            }
-        const double d[3] = {b.Tr[0] - PT[0], b.Tr[1] - PT[1], b.Tr[2] - PT[2]};
-        rt_mul(o.Tr, PR, d);
-        const double *PTo = b.parent >= 0 ? nodes[b.parent].To : Z;
-        const double dO[3] = {b.To[0] - PTo[0], b.To[1] - PTo[1], b.To[2] - PTo[2]};
-        rt_mul(out.obbs[i].To, PR, dO);
-        for (int k = 0; k < 3; k++) out.obbs[i].d[k] = b.d[k];
-        o.l[0] = b.l[0];
-        o.l[1] = b.l[1];
-        o.r = b.r;
-        o.angR = b.angR;
-        o.size = std::sqrt(b.l[0] * b.l[0] + b.l[1] * b.l[1]) + 2 * b.r;
-        o.first_child = b.first_child;
-        o.depth = b.depth;
-        if (b.depth > out.depth) out.depth = b.depth;
-    }
-    for (int32_t i = 0; i < num_tris; i++) {
-        TriRec &t = out.tris[i];
-        std::memcpy(t.v, tris[i].p, sizeof(t.v));
-        t.id = tris[i].id;
-        for (int k = 0; k < 3; k++) t.idx[k] = tris[i].idx[k];
-    }
-    bool ok = true;
-    out.snodes.assign((size_t)num_nodes, NodeShadow{});
-    for (int32_t i = 0; i < num_nodes; i++) {
-        const NodeRec &n = out.nodes[i];
-        NodeShadow &s = out.snodes[i];
-        for (int k = 0; k < 9; k++) {
-            s.R[k] = shadow_of(n.R[k], ok);
-            s.Rloc[k] = shadow_of(n.Rloc[k], ok);
+void BuildThreads::give() { free_.fetch_add(1, std::memory_order_acq_rel); }
+
+namespace {
+
+constexpr int kMaxParts = 64;           /* at most this many threads per record pass */
+constexpr int64_t kPartMin = 16384;     /* records a thread of such a pass handles at least */
+
+/* body(part, lo, hi) over [0, n) in contiguous parts: part 0 on the calling
+ * thread, the others on threads taken from the budget (given back after) */
+template <class Body> void parallel_parts(int64_t n, BuildThreads *threads, Body body)
+{
+    int extra = 0;
+    while (threads && extra + 1 < kMaxParts && (int64_t)(extra + 2) * kPartMin <= n && threads->take()) extra++;
+    const int parts = extra + 1;
+    std::vector<std::thread> pool;
+    std::vector<int> here; // parts no thread could be started for
+    pool.reserve(parts);
+    here.reserve(parts);
+    for (int p = 1; p < parts; p++) {
+        const int64_t lo = n * p / parts, hi = n * (p + 1) / parts;
+        try {
+            pool.emplace_back([&body, p, lo, hi] { body(p, lo, hi); });
+        } catch (const std::exception &) {
+            here.push_back(p);
         }
-        for (int k = 0; k < 3; k++) s.Tr[k] = shadow_of(n.Tr[k], ok);
-        s.l[0] = shadow_of(n.l[0], ok);
-        s.l[1] = shadow_of(n.l[1], ok);
-        s.r = shadow_of(n.r, ok);
-        s.angR = shadow_of(n.angR, ok);
     }
-    out.stris.assign((size_t)num_tris, TriShadow{});
-    for (int32_t i = 0; i < num_tris; i++)
-        for (int k = 0; k < 9; k++) out.stris[i].v[k] = shadow_of(out.tris[i].v[k], ok);
+    body(0, 0, n / parts);
+    for (int p : here) body(p, n * p / parts, n * (p + 1) / parts);
+    for (std::thread &th : pool) th.join();
+    for (int p = 0; p < extra; p++) threads->give();
+}
+
+int build_unchecked(int32_t num_tris, const double *tv, const int32_t *ids, const int32_t *vidx, BuiltModel &out,
+                    BuildThreads *threads)
+{
+    RecordVec<Tri> tris((size_t)num_tris);
+    parallel_parts(num_tris, threads, [&](int, int64_t lo, int64_t hi) {
+        for (int64_t i = lo; i < hi; i++) {
+            std::memcpy(tris[i].p, tv + 9 * (size_t)i, sizeof(tris[i].p));
+            tris[i].id = ids ? ids[i] : (int32_t)i;
+            for (int k = 0; k < 3; k++) tris[i].idx[k] = vidx ? vidx[3 * (size_t)i + k] : -1;
+        }
+    });
+    const int32_t num_nodes = 2 * num_tris - 1;
+    RecordVec<AbsNode> nodes((size_t)num_nodes); // every field set by the build
+    {
+        Builder b(tris, nodes, threads);
+        b.run();
+        if (b.failed()) return C2A_ERR_OUT_OF_MEMORY;
+    }
+
+    // resized without clearing: the passes below write every byte
+    out.nodes.resize((size_t)num_nodes);
+    out.obbs.resize((size_t)num_nodes);
+    out.tris.resize((size_t)num_tris);
+    out.snodes.resize((size_t)num_nodes);
+    out.stris.resize((size_t)num_tris);
+    // every node and triangle record depends on its own node (and parent) only
+    std::vector<int32_t> part_depth(kMaxParts, 0);
+    std::vector<char> part_ok(kMaxParts, 1);
+    parallel_parts(num_nodes, threads, [&](int part, int64_t lo, int64_t hi) {
+        bool ok = true;
+        int32_t depth = 0;
+        for (int64_t i = lo; i < hi; i++) {
+            const AbsNode &b = nodes[i];
+            NodeRec &o = out.nodes[i];
+            // parent-relative frame: R = Rp^T R, Tr = Rp^T (Tr - Trp); the root is
+            // taken relative to the identity exactly as the reference does
+            static const double I[3][3] = {{1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+            static const double Z[3] = {0.0, 0.0, 0.0};
+            const double(*PR)[3] = b.parent >= 0 ? nodes[b.parent].R : I;
+            const double *PT = b.parent >= 0 ? nodes[b.parent].Tr : Z;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) {
+                    o.R[3 * r + c] = PR[0][r] * b.R[0][c] + PR[1][r] * b.R[1][c] + PR[2][r] * b.R[2][c];
+                    o.Rloc[3 * r + c] = b.R[r][c];
+                }
+            const double d[3] = {b.Tr[0] - PT[0], b.Tr[1] - PT[1], b.Tr[2] - PT[2]};
+            rt_mul(o.Tr, PR, d);
+            const double *PTo = b.parent >= 0 ? nodes[b.parent].To : Z;
+            const double dO[3] = {b.To[0] - PTo[0], b.To[1] - PTo[1], b.To[2] - PTo[2]};
+            rt_mul(out.obbs[i].To, PR, dO);
+            for (int k = 0; k < 3; k++) out.obbs[i].d[k] = b.d[k];
+            o.l[0] = b.l[0];
+            o.l[1] = b.l[1];
+            o.r = b.r;
+            o.angR = b.angR;
+            o.size = std::sqrt(b.l[0] * b.l[0] + b.l[1] * b.l[1]) + 2 * b.r;
+            o.first_child = b.first_child;
+            o.depth = b.depth;
+            std::memset(o.pad, 0, sizeof(o.pad));
+            if (b.depth > depth) depth = b.depth;
+            NodeShadow &sh = out.snodes[i];
+            for (int k = 0; k < 9; k++) {
+                sh.R[k] = shadow_of(o.R[k], ok);
+                sh.Rloc[k] = shadow_of(o.Rloc[k], ok);
+            }
+            for (int k = 0; k < 3; k++) sh.Tr[k] = shadow_of(o.Tr[k], ok);
+            sh.l[0] = shadow_of(o.l[0], ok);
+            sh.l[1] = shadow_of(o.l[1], ok);
+            sh.r = shadow_of(o.r, ok);
+            sh.angR = shadow_of(o.angR, ok);
+            std::memset(sh.pad, 0, sizeof(sh.pad));
+        }
+        part_depth[part] = depth;
+        part_ok[part] = ok;
+    });
+    out.depth = 0;
+    bool ok = true;
+    for (int p = 0; p < kMaxParts; p++) {
+        if (part_depth[p] > out.depth) out.depth = part_depth[p];
+        ok = ok && part_ok[p];
+    }
+    std::fill(part_ok.begin(), part_ok.end(), 1);
+    parallel_parts(num_tris, threads, [&](int part, int64_t lo, int64_t hi) {
+        bool tok = true;
+        for (int64_t i = lo; i < hi; i++) {
+            TriRec &t = out.tris[i];
+            std::memcpy(t.v, tris[i].p, sizeof(t.v));
+            t.id = tris[i].id;
+            for (int k = 0; k < 3; k++) t.idx[k] = tris[i].idx[k];
+            t.pad = 0.0;
+            for (int k = 0; k < 9; k++) out.stris[i].v[k] = shadow_of(t.v[k], tok);
+            std::memset(out.stris[i].pad, 0, sizeof(out.stris[i].pad));
+        }
+        part_ok[part] = tok;
+    });
+    for (int p = 0; p < kMaxParts; p++) ok = ok && part_ok[p];
     out.shadow_ok = ok;
     return 0;
+}
+
+} // namespace
+
+int build_rss_model(int32_t num_tris, const double *tv, const int32_t *ids, const int32_t *vidx, BuiltModel &out,
+                    BuildThreads *threads)
+{
+    if (num_tris <= 0 || !tv) return C2A_ERR_EMPTY_MODEL;
+    try {
+        return build_unchecked(num_tris, tv, ids, vidx, out, threads);
+    } catch (const std::bad_alloc &) {
+        out = BuiltModel{};
+        return C2A_ERR_OUT_OF_MEMORY;
+    }
 }
 
 } // namespace c2a

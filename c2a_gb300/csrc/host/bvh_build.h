@@ -5,7 +5,11 @@
 #ifndef C2A_BVH_BUILD_H
 #define C2A_BVH_BUILD_H
 
+#include <atomic>
 #include <cstdint>
+#include <memory>
+#include <new>
+#include <utility>
 #include <vector>
 
 namespace c2a {
@@ -68,19 +72,47 @@ struct alignas(16) ObbRec {
 };
 static_assert(sizeof(ObbRec) == 48, "OBB record must stay 48 bytes");
 
+/* std::allocator whose value-less construct leaves a record unset, so that
+ * resize() does not clear memory the build then writes in full on parallel
+ * threads (each page is first touched by the thread that fills it) */
+template <class T> struct RecordAlloc : std::allocator<T> {
+    template <class U> struct rebind {
+        using other = RecordAlloc<U>;
+    };
+    RecordAlloc() = default;
+    template <class U> RecordAlloc(const RecordAlloc<U> &) noexcept {}
+    template <class U> void construct(U *p) noexcept { ::new ((void *)p) U; }
+    template <class U, class... A> void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+template <class T> using RecordVec = std::vector<T, RecordAlloc<T>>;
+
 struct BuiltModel {
-    std::vector<ObbRec> obbs;
-    std::vector<NodeRec> nodes;
-    std::vector<TriRec> tris;
-    std::vector<NodeShadow> snodes;
-    std::vector<TriShadow> stris;
+    RecordVec<ObbRec> obbs;
+    RecordVec<NodeRec> nodes;
+    RecordVec<TriRec> tris;
+    RecordVec<NodeShadow> snodes;
+    RecordVec<TriShadow> stris;
     bool shadow_ok = true; /* every shadowed value lies in FP32's normal range (or is 0) */
     int32_t depth = 0;     /* maximum node depth (root = 0) */
 };
 
-/* C2A_Model::EndModel + C2A_BuildModel: returns 0 or a C2A_ERR_* code. */
+/* Host threads a build may start for its subtrees, beyond the calling one;
+ * one budget can be shared by builds running at the same time. */
+class BuildThreads {
+  public:
+    explicit BuildThreads(int extra) : free_(extra > 0 ? extra : 0) {}
+    bool take(); /* one thread, if any is left */
+    void give(); /* a thread taken before, or one the caller lends */
+
+  private:
+    std::atomic<int> free_;
+};
+
+/* C2A_Model::EndModel + C2A_BuildModel: returns 0 or a C2A_ERR_* code.
+ * threads: the budget for subtree threads (nullptr: this thread only); the
+ * tree is the same either way. */
 int build_rss_model(int32_t num_tris, const double *tri_verts, const int32_t *ids, const int32_t *vidx,
-                    BuiltModel &out);
+                    BuiltModel &out, BuildThreads *threads = nullptr);
 
 /* Symmetric 3x3 eigen-decomposition (columns of v are eigenvectors). */
 void jacobi_eigen3(double v[3][3], double d[3], const double a[3][3]);

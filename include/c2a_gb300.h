@@ -197,9 +197,22 @@ c2a_status c2a_launch_count(c2a_context *ctx, int64_t *count);
 /* ---- models ---------------------------------------------------------- */
 /* Builds the RSS hierarchy of a triangle soup on the host (bit-identical to
  * the reference's EndModel) and uploads it.  tri_verts: num_tris x 9 doubles
- * (p1, p2, p3); ids and vidx (num_tris x 3) may be NULL. */
+ * (p1, p2, p3); ids and vidx (num_tris x 3) may be NULL.  Subtrees of 4,096
+ * triangles or more build on parallel host threads (C2A_BUILD_THREADS, else
+ * every hardware thread); the tree does not depend on the thread count. */
 c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
                            const int32_t *vidx, int32_t *model_id);
+/* c2a_model_build over count models at once (the reference builds each
+ * C2A_Model on its own, C2A/src/C2A_PQP.cpp:332-417): the models build on
+ * parallel host threads, largest first, and a model's subtrees split over
+ * the threads the others leave free.  threads: host threads to use, 0 for
+ * C2A_BUILD_THREADS or else every hardware thread.  ids and vidx may be NULL,
+ * or hold NULL entries.  model_ids[i] is model i's id, in the order given;
+ * every tree is bit-identical to a c2a_model_build of the same model.  On an
+ * error no model of the call is kept. */
+c2a_status c2a_model_build_many(c2a_context *ctx, int32_t count, const int32_t *num_tris,
+                                const double *const *tri_verts, const int32_t *const *ids,
+                                const int32_t *const *vidx, int32_t threads, int32_t *model_ids);
 c2a_status c2a_model_info(c2a_context *ctx, int32_t model_id, int32_t *num_tris, int32_t *num_nodes,
                           int32_t *depth);
 /* Host copy of the built hierarchy: node_f num_nodes x 25 doubles (R 9, Tr 3,

@@ -128,6 +128,61 @@ def test_bvh_matches_port_on_degenerate_soups(lib, port):
             assert bits(tv) == bits(tris["v"]), m.name
 
 
+def _model_digest(ctx, mid):
+    dig = hashlib.sha256()
+    for a in ctx.download(mid):
+        dig.update(np.ascontiguousarray(a).tobytes())
+    dig.update(ctx.download_obb(mid).tobytes())
+    return dig.hexdigest()
+
+
+def test_threaded_build_is_bit_identical(lib, monkeypatch):
+    """Subtrees split over host threads (a 40,000-triangle knot spawns them at
+    4,096 triangles), alone or beside other models in c2a_model_build_many:
+    the same tree whatever the thread count."""
+    from c2a_gb300 import api, meshes
+
+    ms = [meshes.torus_knot(2, 3, 400, 50), meshes.triangle_soup(9000, seed=5), meshes.torus_knot(3, 5, 60, 12),
+          meshes.icosphere(3, noise=0.02, seed=3)]
+    want = {}
+    monkeypatch.setenv("C2A_BUILD_THREADS", "1")
+    with api.Context(-1) as ctx:
+        for m in ms:
+            want[m.name] = _model_digest(ctx, ctx.model(m))
+    for threads in ("2", "7", "16"):
+        monkeypatch.setenv("C2A_BUILD_THREADS", threads)
+        with api.Context(-1) as ctx:
+            got = _model_digest(ctx, ctx.model(ms[0]))
+        assert got == want[ms[0].name], threads
+    for threads in (1, 3, 8):
+        with api.Context(-1) as ctx:
+            mid0 = ctx.model(ms[3])
+            ids = ctx.models(ms, threads=threads)
+            assert ids == [mid0 + 1 + i for i in range(len(ms))]
+            assert [_model_digest(ctx, i) for i in ids] == [want[m.name] for m in ms], threads
+
+
+def test_build_many_rejects_bad_input_and_keeps_nothing(lib):
+    import ctypes as C
+    from c2a_gb300 import api, meshes
+
+    knot = meshes.torus_knot(2, 3, 12, 4)
+    tv = knot.tri_verts()
+    with api.Context(-1) as ctx:
+        counts = np.array([knot.num_tris, 0], dtype=np.int32)
+        ptrs = (C.c_void_p * 2)(tv.ctypes.data, tv.ctypes.data)
+        ids = np.full(2, -1, dtype=np.int32)
+        pp = C.cast(ptrs, C.c_void_p)
+        assert lib.c2a_model_build_many(ctx.h, 2, api._ptr(counts), pp, None, None, 0, api._ptr(ids)) == \
+            api.ERR_EMPTY_MODEL
+        assert lib.c2a_model_build_many(ctx.h, -1, None, None, None, None, 0, None) == api.ERR_INVALID_ARGUMENT
+        assert lib.c2a_model_build_many(ctx.h, 1, api._ptr(counts), pp, None, None, -2, api._ptr(ids)) == \
+            api.ERR_INVALID_ARGUMENT
+        assert lib.c2a_model_build_many(ctx.h, 0, None, None, None, None, 0, None) == api.OK
+        assert ctx.models([]) == []
+        assert ctx.model(knot) == 0  # the failed calls kept no model
+
+
 def test_motion_matches_reference(lib):
     """CInterpMotion_Linear constants and integrate() (InterpMotion.cpp:228-287,
     486-568) against the reference, bit for bit."""
