@@ -26,7 +26,8 @@ oracle's own arithmetic) against the FP64 peak measured in the same run.
 cpu_baseline: the oracle port on all host cores over a strided sample,
 compared with the GPU's results field by field and contact by contact.
 --impl reference: the CPU oracle port of the reference (bit-identical to
-the reference's own code) on all host cores, on a bounded sample.
+the reference's own code) on all host cores, on a bounded sample, plus the
+same code on one core (cpu_baseline.single_core) over a smaller sample.
 Under torchrun each rank runs its own replica batch (queries are independent).
 """
 from __future__ import annotations
@@ -198,12 +199,18 @@ def run_reference(args, rank, world):
         times.append(dt)
     value = float(wl.n * len(times) / sum(times))
     sample = f"{wl.n} of the {args.queries} queries, evenly strided, every step"
+    # the same code on one core, over every 16th query of that sample
+    one_idx = all_idx[::16]
+    one_rate, one_dt, _, _ = cpu_baseline(wl, one_idx, 1)
+    single_core = {"value": one_rate, "unit": UNIT, "cores": 1,
+                   "sample": f"{len(one_idx)} of the {args.queries} queries, evenly strided, once ({one_dt:.1f} s)"}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
             "data": "synthetic: seeded procedural torus knots (the reference publishes no scenes)",
             "config": config_dict(wl, args, queries=args.queries), "implementation": implementation_dict(args),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "single_core": single_core},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
