@@ -162,6 +162,32 @@ def test_threaded_build_is_bit_identical(lib, monkeypatch):
             assert [_model_digest(ctx, i) for i in ids] == [want[m.name] for m in ms], threads
 
 
+def test_threaded_build_matches_port_on_large_degenerate_soups(lib, port, monkeypatch):
+    """Splits that fall back to n/2 (every centroid on one side) and repeated
+    triangles, large enough that subtrees go to other threads: the threaded
+    build against the oracle's sequential one."""
+    from c2a_gb300 import api, meshes
+
+    rng = np.random.default_rng(11)
+    tri = rng.normal(size=(3, 3))
+    same = np.tile(tri, (12000, 1))  # 12,000 copies of one triangle
+    mixed = np.concatenate([same[:9000 * 3], rng.normal(size=(3 * 9000, 3))])
+    cases = [meshes.Mesh(name, v, np.arange(len(v), dtype=np.int32).reshape(-1, 3), v, 0.0)
+             for name, v in (("copies", same), ("copies+soup", mixed))]
+    monkeypatch.setenv("C2A_BUILD_THREADS", "8")
+    with api.Context(-1) as ctx:
+        ids = ctx.models(cases, threads=8)
+        for m, mid in zip(cases, ids):
+            f, fc, tv, tid, tidx = ctx.download(mid)
+            nodes, tris = port.dump(port.models([m]), 0)
+            pf = np.concatenate([nodes["R"], nodes["Tr"], nodes["l"], nodes["r"][:, None], nodes["angR"][:, None],
+                                 nodes["Rloc"]], axis=1)
+            assert bits(f) == bits(pf), m.name
+            assert np.array_equal(fc, nodes["first_child"]), m.name
+            assert bits(tv) == bits(tris["v"]), m.name
+            assert ctx.model_info(mid)[2] == int(np.ceil(np.log2(m.num_tris))) or m.name != "copies"
+
+
 def test_build_many_rejects_bad_input_and_keeps_nothing(lib):
     import ctypes as C
     from c2a_gb300 import api, meshes
