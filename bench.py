@@ -80,8 +80,9 @@ def parse():
     p.add_argument("--epochs", type=int, default=6, help="--mode learned: training epochs")
     p.add_argument("--engine", choices=["auto", "warp", "thread", "batched", "spec"], default="auto")
     p.add_argument("--order", choices=["learned", "geometric"], default="learned",
-                   help="REFERENCE mode: the work-queue order; learned: a cost model trained on another seed's "
-                        "queries (costs measured by the library) starts the costliest queries first; geometric: "
+                   help="REFERENCE mode: the work-queue order; learned: a cost model trained on other seeds' "
+                        "batches (--order-seeds; costs measured by the library) starts the costliest queries "
+                        "first; geometric: "
                         "queries whose bounding spheres approach first.  Results are identical either way.")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--heavy", type=int, default=0,
