@@ -355,7 +355,41 @@ class SeedNet:
         return idx.cpu().numpy()
 
     def state(self) -> dict:
-        return {f"p{i}": p.cpu().numpy() for i, p in enumerate(self.params)}
+        """Weights, biases and mesh embeddings (float32), then the Adam moments
+        and step: everything training needs to resume."""
+        st = {f"p{i}": p.cpu().numpy() for i, p in enumerate(self.params)}
+        st.update({f"m{i}": m.cpu().numpy() for i, m in enumerate(self.m)})
+        st.update({f"v{i}": v.cpu().numpy() for i, v in enumerate(self.v)})
+        st["t"] = np.int64(self.t)
+        return st
+
+    def save(self, path: str) -> None:
+        """Checkpoint to one .npz (state())."""
+        np.savez(path, **self.state())
+
+    def load_state(self, st) -> None:
+        """Restores state() (shapes must match); the BF16 weight copies the
+        GEMMs read are re-derived from the FP32 weights."""
+        torch = self.torch
+        for name, group in (("p", self.params), ("m", self.m), ("v", self.v)):
+            for i, t in enumerate(group):
+                a = np.asarray(st[f"{name}{i}"], dtype=np.float32)
+                if a.shape != tuple(t.shape):
+                    raise ValueError(f"checkpoint {name}{i} has shape {a.shape}, the network {tuple(t.shape)}")
+                t.copy_(torch.from_numpy(a))
+        self.t = int(st["t"])
+        for i, w in enumerate(self.W):
+            self.Wb[i].copy_(w.to(torch.bfloat16))
+            self.WbT[i].copy_(w.t().contiguous().to(torch.bfloat16))
+
+    @classmethod
+    def load(cls, path: str, device: str = "cuda") -> "SeedNet":
+        """A network rebuilt from save()'s checkpoint (its mesh count read from it)."""
+        with np.load(path) as z:
+            st = {k: z[k] for k in z.files}
+        net = cls(int(st["p8"].shape[0]), device=device)
+        net.load_state(st)
+        return net
 
 
 def solve_hinted(ctx: api.Context, qint: np.ndarray, poses: np.ndarray, params: dict, hints: np.ndarray,
@@ -519,9 +553,22 @@ class CostOrder:
     first), which shortens a batch whose length is set by its heaviest
     queries.  The order never changes a result (c2a_solve_batch_ordered)."""
 
-    def __init__(self, num_meshes: int = 1, seed: int = 0):
-        self.net = SeedNet(num_meshes, seed=seed)
+    def __init__(self, num_meshes: int = 1, seed: int = 0, device: str = "cuda"):
+        self.net = SeedNet(num_meshes, seed=seed, device=device)
         self.top = 1.0
+
+    def save(self, path: str) -> None:
+        """Checkpoint: the network's state and the cost scale of the buckets."""
+        np.savez(path, top=np.float64(self.top), **self.net.state())
+
+    @classmethod
+    def load(cls, path: str, device: str = "cuda") -> "CostOrder":
+        with np.load(path) as z:
+            st = {k: z[k] for k in z.files}
+        co = cls(int(st["p8"].shape[0]), device=device)
+        co.net.load_state(st)
+        co.top = float(st["top"])
+        return co
 
     def fit(self, feat, ia, ib, cost, epochs: int = 10, batch: int = 1024, log=None) -> list[float]:
         y = np.log1p(np.asarray(cost, dtype=np.float64))

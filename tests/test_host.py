@@ -188,6 +188,35 @@ def test_threaded_build_matches_port_on_large_degenerate_soups(lib, port, monkey
             assert ctx.model_info(mid)[2] == int(np.ceil(np.log2(m.num_tris))) or m.name != "copies"
 
 
+@pytest.mark.parametrize("sanitizer", ["thread", "address,undefined"])
+def test_threaded_build_under_sanitizer(tmp_path, sanitizer):
+    """The threaded build (subtree threads, record passes, the thread budget)
+    compiled with ThreadSanitizer, then AddressSanitizer + UBSan, against
+    the sequential build of the same 40,000-triangle knot: no report, and
+    the same bytes in every record."""
+    import shutil
+    import subprocess
+
+    from c2a_gb300 import meshes
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    knot = meshes.torus_knot(2, 3, 400, 50)
+    soup = tmp_path / "knot.bin"
+    with open(soup, "wb") as f:
+        f.write(np.int32(knot.num_tris).tobytes())
+        f.write(np.ascontiguousarray(knot.tri_verts()).tobytes())
+    exe = str(tmp_path / "build_race")
+    subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fno-omit-frame-pointer", "-ffp-contract=off",
+                    f"-fsanitize={sanitizer}", "-fno-sanitize-recover=all", "-pthread", "-o", exe,
+                    os.path.join(ROOT, "tests", "cpp", "build_race.cpp"),
+                    os.path.join(ROOT, "c2a_gb300", "csrc", "host", "bvh_build.cpp")], check=True)
+    env = dict(os.environ, TSAN_OPTIONS="halt_on_error=1", ASAN_OPTIONS="halt_on_error=1:detect_leaks=1",
+               UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([exe, str(soup), "8"], capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0 and r.stdout.startswith("same"), r.stdout + r.stderr[-4000:]
+
+
 def test_build_many_rejects_bad_input_and_keeps_nothing(lib):
     import ctypes as C
     from c2a_gb300 import api, meshes

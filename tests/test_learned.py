@@ -105,6 +105,36 @@ def to_bf16_np(a):
     return mlp_ref.bf16(a)
 
 
+def test_checkpoint_round_trip(lib, tmp_path):
+    """SeedNet and CostOrder checkpoints restore every weight, embedding,
+    Adam moment and the step, and re-derive the BF16 copies the GEMMs read."""
+    import torch
+
+    rng = np.random.default_rng(9)
+    net = learned.SeedNet(5, seed=1, device="cpu")
+    for group in (net.params, net.m, net.v):
+        for t in group:
+            t.copy_(torch.from_numpy(rng.normal(size=tuple(t.shape)).astype(np.float32)))
+    net.t = 17
+    net.save(str(tmp_path / "net.npz"))
+    back = learned.SeedNet.load(str(tmp_path / "net.npz"), device="cpu")
+    assert back.t == 17 and back.E.shape == (5, learned.EMBED)
+    for a, b in zip(net.params + net.m + net.v, back.params + back.m + back.v):
+        assert torch.equal(a, b)
+    for i, w in enumerate(net.W):
+        assert torch.equal(back.Wb[i], w.to(torch.bfloat16))
+        assert torch.equal(back.WbT[i], w.t().contiguous().to(torch.bfloat16))
+    with pytest.raises(ValueError):
+        learned.SeedNet(4, device="cpu").load_state(net.state())  # another mesh count
+
+    co = learned.CostOrder(2, seed=3, device="cpu")
+    co.top = 6.25
+    co.save(str(tmp_path / "cost.npz"))
+    co2 = learned.CostOrder.load(str(tmp_path / "cost.npz"), device="cpu")
+    assert co2.top == 6.25
+    assert all(torch.equal(a, b) for a, b in zip(co.net.params, co2.net.params))
+
+
 @pytest.mark.gpu
 def test_gpu_gemm_matches_numpy(gpu_ctx):
     import torch
