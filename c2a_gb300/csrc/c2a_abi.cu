@@ -5,6 +5,7 @@
  * does), moves buffers and launches.
  */
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdio>
@@ -31,6 +32,20 @@ using namespace c2a;
 #ifndef C2A_SPEC_EXTRA
 #define C2A_SPEC_EXTRA 64
 #endif
+
+namespace {
+
+/* an NVTX range over an entry point, for profilers (nvtxRangePushA/Pop cost
+ * a few nanoseconds and do nothing unless a tool is attached) */
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+#define C2A_RANGE(name) NvtxRange c2a_range_(name)
+
+} // namespace
 
 namespace {
 
@@ -473,6 +488,7 @@ c2a_status register_model(c2a_context *ctx, ModelSlot &slot, int32_t *model_id)
 c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
                            const int32_t *vidx, int32_t *model_id)
 {
+    C2A_RANGE("c2a_model_build");
     if (!ctx || !model_id) return C2A_ERR_INVALID_ARGUMENT;
     ModelSlot slot;
     BuildThreads threads(build_thread_count(0) - 1);
@@ -486,6 +502,7 @@ c2a_status c2a_model_build_many(c2a_context *ctx, int32_t count, const int32_t *
                                 const double *const *tri_verts, const int32_t *const *ids,
                                 const int32_t *const *vidx, int32_t threads, int32_t *model_ids)
 {
+    C2A_RANGE("c2a_model_build_many");
     if (!ctx || count < 0 || (count > 0 && (!num_tris || !tri_verts || !model_ids)) || threads < 0)
         return C2A_ERR_INVALID_ARGUMENT;
     for (int32_t i = 0; i < count; i++)
@@ -622,6 +639,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
 c2a_status c2a_solve_batch_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n, const c2a_params *params,
                                   c2a_result *d_results, c2a_contact *d_contacts, void *stream)
 {
+    C2A_RANGE("c2a_solve_batch_device");
     return solve_device(ctx, d_queries, n, params, d_results, d_contacts, stream, nullptr, 0);
 }
 
@@ -629,6 +647,7 @@ c2a_status c2a_solve_batch_ordered(c2a_context *ctx, const c2a_query *d_queries,
                                    const c2a_params *params, const int32_t *d_order, c2a_result *d_results,
                                    c2a_contact *d_contacts, void *stream)
 {
+    C2A_RANGE("c2a_solve_batch_ordered");
     if (!params || params->mode != C2A_MODE_REFERENCE ||
         (params->engine != C2A_ENGINE_AUTO && params->engine != C2A_ENGINE_WARP &&
          params->engine != C2A_ENGINE_SPEC) ||
@@ -641,6 +660,7 @@ c2a_status c2a_solve_batch_hinted(c2a_context *ctx, const c2a_query *d_queries, 
                                   const uint32_t *d_hints, int32_t hints_per_query, c2a_result *d_results,
                                   c2a_contact *d_contacts, void *stream)
 {
+    C2A_RANGE("c2a_solve_batch_hinted");
     if (!params || params->mode != C2A_MODE_CANONICAL || hints_per_query < 0 || hints_per_query > 16 ||
         (hints_per_query > 0 && !d_hints))
         return C2A_ERR_INVALID_ARGUMENT;
@@ -805,6 +825,7 @@ c2a_status solve_device(c2a_context *ctx, const c2a_query *d_queries, int32_t n,
 
 c2a_status c2a_distance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, c2a_distance_result *results)
 {
+    C2A_RANGE("c2a_distance_batch");
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || (n > 0 && (!queries || !results))) return C2A_ERR_INVALID_ARGUMENT;
     if (n == 0) return C2A_OK;
@@ -899,6 +920,7 @@ c2a_status solve_host(c2a_context *ctx, const c2a_query *queries, int32_t n, con
 c2a_status c2a_solve_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const c2a_params *params,
                            c2a_result *results, c2a_contact *contacts)
 {
+    C2A_RANGE("c2a_solve_batch");
     return solve_host(ctx, queries, n, params, results, contacts, nullptr);
 }
 
@@ -906,6 +928,7 @@ c2a_status c2a_solve_batch_ordered_host(c2a_context *ctx, const c2a_query *queri
                                         const c2a_params *params, const int32_t *d_order, c2a_result *results,
                                         c2a_contact *contacts)
 {
+    C2A_RANGE("c2a_solve_batch_ordered_host");
     if (n > 0 && !d_order) return C2A_ERR_INVALID_ARGUMENT;
     return solve_host(ctx, queries, n, params, results, contacts, d_order);
 }
@@ -914,6 +937,7 @@ c2a_status c2a_solve_batch_noalloc(c2a_context *ctx, const c2a_query *d_queries,
                                    const c2a_params *params, c2a_result *d_results, c2a_contact *d_contacts,
                                    void *stream)
 {
+    C2A_RANGE("c2a_solve_batch_noalloc");
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || !params_ok(params) || (n > 0 && (!d_queries || !d_results))) return C2A_ERR_INVALID_ARGUMENT;
     if (n == 0) return C2A_OK;
@@ -988,6 +1012,7 @@ c2a_status static_prepare(c2a_context *ctx, const c2a_query *queries, int32_t n)
 c2a_status c2a_tolerance_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *tolerance,
                                c2a_tolerance_result *results)
 {
+    C2A_RANGE("c2a_tolerance_batch");
     if (n > 0 && (!tolerance || !results)) return C2A_ERR_INVALID_ARGUMENT;
     if (ctx) {
         std::lock_guard<std::mutex> lock(ctx->mu);
@@ -1021,6 +1046,7 @@ c2a_status c2a_tolerance_batch(c2a_context *ctx, const c2a_query *queries, int32
 c2a_status c2a_collide_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, int32_t flag,
                              int32_t pairs_per_query, c2a_collide_result *results, int32_t *pairs)
 {
+    C2A_RANGE("c2a_collide_batch");
     if (n > 0 && !results) return C2A_ERR_INVALID_ARGUMENT;
     if (pairs_per_query < 0 || (flag != 1 && flag != 2)) return C2A_ERR_INVALID_ARGUMENT;
     if (!ctx) return C2A_ERR_INVALID_ARGUMENT;
@@ -1056,6 +1082,7 @@ c2a_status c2a_toc_step_batch(c2a_context *ctx, const c2a_query *queries, int32_
                               const int32_t *num_ca, const double *prev_mint, const c2a_params *params,
                               c2a_result *results)
 {
+    C2A_RANGE("c2a_toc_step_batch");
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || !params_ok(params) || params->mode != C2A_MODE_REFERENCE ||
         (n > 0 && (!queries || !lambda || !num_ca || !prev_mint || !results)))
@@ -1096,6 +1123,7 @@ c2a_status c2a_toc_step_batch(c2a_context *ctx, const c2a_query *queries, int32_
 c2a_status c2a_contact_only_batch(c2a_context *ctx, const c2a_query *queries, int32_t n, const double *threshold,
                                   int32_t contacts_per_query, c2a_result *results, c2a_contact *contacts)
 {
+    C2A_RANGE("c2a_contact_only_batch");
     if (ctx && ctx->device < 0) return C2A_ERR_NO_DEVICE;
     if (!ctx || n < 0 || contacts_per_query < 0 || (n > 0 && (!queries || !threshold || !results)))
         return C2A_ERR_INVALID_ARGUMENT;
