@@ -28,7 +28,9 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <thread>
@@ -95,46 +97,117 @@ class Builder {
     {
     }
 
-    void run() { build_from({0, 0, (int32_t)tris_.size(), -1, 0, 1}, false); }
+    void run()
+    {
+        const BuildTask root{0, 0, (int32_t)tris_.size(), -1, 0, 1};
+        if (!threads_ || root.count < 2 * kSpawnGrain) {
+            std::vector<double> proj;
+            guarded_subtree(root, proj, nullptr);
+            return;
+        }
+        Pool pool;
+        pool.queue.push_back(root);
+        pool.pending = 1;
+        work(pool); // returns once every task is done
+        std::vector<std::thread> workers;
+        {
+            std::lock_guard<std::mutex> lock(pool.mu);
+            workers.swap(pool.workers);
+        }
+        for (std::thread &th : workers) th.join();
+    }
 
   private:
-    /* builds the subtree of task t depth first, left before right; a right
-     * subtree of at least kSpawnGrain triangles goes to a new thread when the
-     * budget has one to spare.  holds_thread: this call runs on a thread
-     * taken from the budget, given back once its own work is done. */
-    void build_from(BuildTask t0, bool holds_thread)
+    /* the subtrees waiting for a thread, shared by the build's threads: at
+     * most the calling thread plus those taken from the budget, each giving
+     * its thread back when the whole tree is done */
+    struct Pool {
+        std::mutex mu;
+        std::condition_variable cv;
+        std::vector<BuildTask> queue;
+        int pending = 0; /* tasks queued or running */
+        int idle = 0;    /* threads waiting for a task */
+        std::vector<std::thread> workers;
+    };
+
+    void work(Pool &pool)
     {
-        std::vector<std::thread> spawned;
-        try {
-            std::vector<double> proj;
-            std::vector<BuildTask> stack;
-            stack.push_back(t0);
-            while (!stack.empty()) {
-                const BuildTask t = stack.back();
-                stack.pop_back();
-                const int32_t nleft = fit_and_split(t, proj);
-                if (t.count == 1) continue;
-                // a subtree of k triangles allocates 2k - 2 nodes below its root
-                const BuildTask left{t.base, t.first, nleft, t.node, t.depth + 1, t.base + 2};
-                const BuildTask right{t.base + 1, t.first + nleft, t.count - nleft, t.node, t.depth + 1,
-                                      t.base + 2 * nleft};
-                bool handed_off = false;
-                if (threads_ && right.count >= kSpawnGrain && threads_->take()) {
-                    try {
-                        spawned.emplace_back([this, right] { build_from(right, true); });
-                        handed_off = true;
-                    } catch (const std::exception &) { // no thread (system_error) or no room to keep it
-                        threads_->give();
-                    }
+        std::vector<double> proj;
+        for (;;) {
+            BuildTask t;
+            {
+                std::unique_lock<std::mutex> lock(pool.mu);
+                while (pool.queue.empty() && pool.pending > 0) {
+                    pool.idle++;
+                    pool.cv.wait(lock);
+                    pool.idle--;
                 }
-                if (!handed_off) stack.push_back(right);
-                stack.push_back(left);
+                if (pool.queue.empty()) return; // nothing queued, nothing running: done
+                t = pool.queue.back();
+                pool.queue.pop_back();
             }
+            guarded_subtree(t, proj, &pool);
+            std::lock_guard<std::mutex> lock(pool.mu);
+            if (--pool.pending == 0) pool.cv.notify_all();
+        }
+    }
+
+    /* queues subtree t for another thread when one waits for work or can be
+     * taken from the budget; false: the caller builds it */
+    bool share(Pool &pool, const BuildTask &t)
+    {
+        std::lock_guard<std::mutex> lock(pool.mu);
+        const bool start = pool.idle <= (int)pool.queue.size();
+        if (start && !threads_->take()) return false;
+        try {
+            pool.queue.push_back(t);
+        } catch (const std::bad_alloc &) {
+            if (start) threads_->give();
+            return false;
+        }
+        pool.pending++;
+        if (start) {
+            try {
+                pool.workers.emplace_back([this, &pool] {
+                    work(pool);
+                    threads_->give();
+                });
+            } catch (const std::exception &) { // no thread (system_error) or no room to keep it
+                threads_->give();          // the task waits for a thread already running
+            }
+        }
+        pool.cv.notify_one();
+        return true;
+    }
+
+    void guarded_subtree(const BuildTask &t, std::vector<double> &proj, Pool *pool)
+    {
+        try {
+            build_subtree(t, proj, pool);
         } catch (const std::bad_alloc &) {
             failed_ = true;
         }
-        if (holds_thread) threads_->give();
-        for (std::thread &th : spawned) th.join();
+    }
+
+    /* builds the subtree of task t0 depth first, left before right; with a
+     * pool, a right subtree of at least kSpawnGrain triangles may go to
+     * another thread */
+    void build_subtree(const BuildTask &t0, std::vector<double> &proj, Pool *pool)
+    {
+        std::vector<BuildTask> stack;
+        stack.push_back(t0);
+        while (!stack.empty()) {
+            const BuildTask t = stack.back();
+            stack.pop_back();
+            const int32_t nleft = fit_and_split(t, proj);
+            if (t.count == 1) continue;
+            // a subtree of k triangles allocates 2k - 2 nodes below its root
+            const BuildTask left{t.base, t.first, nleft, t.node, t.depth + 1, t.base + 2};
+            const BuildTask right{t.base + 1, t.first + nleft, t.count - nleft, t.node, t.depth + 1,
+                                  t.base + 2 * nleft};
+            if (!(pool && right.count >= kSpawnGrain && share(*pool, right))) stack.push_back(right);
+            stack.push_back(left);
+        }
     }
 
   public:

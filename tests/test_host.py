@@ -162,6 +162,19 @@ def test_threaded_build_is_bit_identical(lib, monkeypatch):
             assert [_model_digest(ctx, i) for i in ids] == [want[m.name] for m in ms], threads
 
 
+def _chain_soup(n: int, ratio: float = 1.01) -> np.ndarray:
+    """n small triangles at x = -ratio^i: every split at the mean cuts off a
+    few hundred of the farthest, so the tree is a chain of large subtrees
+    (depth ~57 for 40,000 triangles)."""
+    x = -(ratio ** np.arange(n))
+    s = 0.01 * np.abs(x)
+    v = np.zeros((3 * n, 3))
+    v[0::3, 0] = x
+    v[1::3, 0], v[1::3, 1] = x, s
+    v[2::3, 0], v[2::3, 2] = x, s
+    return v
+
+
 def test_threaded_build_matches_port_on_large_degenerate_soups(lib, port, monkeypatch):
     """Splits that fall back to n/2 (every centroid on one side) and repeated
     triangles, large enough that subtrees go to other threads: the threaded
@@ -173,7 +186,7 @@ def test_threaded_build_matches_port_on_large_degenerate_soups(lib, port, monkey
     same = np.tile(tri, (12000, 1))  # 12,000 copies of one triangle
     mixed = np.concatenate([same[:9000 * 3], rng.normal(size=(3 * 9000, 3))])
     cases = [meshes.Mesh(name, v, np.arange(len(v), dtype=np.int32).reshape(-1, 3), v, 0.0)
-             for name, v in (("copies", same), ("copies+soup", mixed))]
+             for name, v in (("copies", same), ("copies+soup", mixed), ("chain", _chain_soup(30000)))]
     monkeypatch.setenv("C2A_BUILD_THREADS", "8")
     with api.Context(-1) as ctx:
         ids = ctx.models(cases, threads=8)
@@ -186,14 +199,15 @@ def test_threaded_build_matches_port_on_large_degenerate_soups(lib, port, monkey
             assert np.array_equal(fc, nodes["first_child"]), m.name
             assert bits(tv) == bits(tris["v"]), m.name
             assert ctx.model_info(mid)[2] == int(np.ceil(np.log2(m.num_tris))) or m.name != "copies"
+            assert ctx.model_info(mid)[2] > 40 or m.name != "chain"
 
 
 @pytest.mark.parametrize("sanitizer", ["thread", "address,undefined"])
 def test_threaded_build_under_sanitizer(tmp_path, sanitizer):
-    """The threaded build (subtree threads, record passes, the thread budget)
-    compiled with ThreadSanitizer, then AddressSanitizer + UBSan, against
-    the sequential build of the same 40,000-triangle knot: no report, and
-    the same bytes in every record."""
+    """The threaded build (the subtree pool, record passes, the thread
+    budget) compiled with ThreadSanitizer, then AddressSanitizer + UBSan,
+    against the sequential build of a 40,000-triangle knot and of a
+    chain-shaped tree: no report, and the same bytes in every record."""
     import shutil
     import subprocess
 
@@ -202,10 +216,12 @@ def test_threaded_build_under_sanitizer(tmp_path, sanitizer):
     if not shutil.which("g++"):
         pytest.skip("no g++")
     knot = meshes.torus_knot(2, 3, 400, 50)
-    soup = tmp_path / "knot.bin"
-    with open(soup, "wb") as f:
-        f.write(np.int32(knot.num_tris).tobytes())
-        f.write(np.ascontiguousarray(knot.tri_verts()).tobytes())
+    soups = []
+    for name, tv in (("knot", knot.tri_verts()), ("chain", _chain_soup(40000).reshape(-1, 9))):
+        soups.append(tmp_path / f"{name}.bin")
+        with open(soups[-1], "wb") as f:
+            f.write(np.int32(len(tv)).tobytes())
+            f.write(np.ascontiguousarray(tv).tobytes())
     exe = str(tmp_path / "build_race")
     subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fno-omit-frame-pointer", "-ffp-contract=off",
                     f"-fsanitize={sanitizer}", "-fno-sanitize-recover=all", "-pthread", "-o", exe,
@@ -213,8 +229,9 @@ def test_threaded_build_under_sanitizer(tmp_path, sanitizer):
                     os.path.join(ROOT, "c2a_gb300", "csrc", "host", "bvh_build.cpp")], check=True)
     env = dict(os.environ, TSAN_OPTIONS="halt_on_error=1", ASAN_OPTIONS="halt_on_error=1:detect_leaks=1",
                UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
-    r = subprocess.run([exe, str(soup), "8"], capture_output=True, text=True, env=env, timeout=600)
-    assert r.returncode == 0 and r.stdout.startswith("same"), r.stdout + r.stderr[-4000:]
+    for soup in soups:
+        r = subprocess.run([exe, str(soup), "8"], capture_output=True, text=True, env=env, timeout=600)
+        assert r.returncode == 0 and r.stdout.startswith("same"), r.stdout + r.stderr[-4000:]
 
 
 def test_build_many_rejects_bad_input_and_keeps_nothing(lib):
