@@ -253,6 +253,36 @@ def test_build_many_rejects_bad_input_and_keeps_nothing(lib):
         assert lib.c2a_model_build_many(ctx.h, 0, None, None, None, None, 0, None) == api.OK
         assert ctx.models([]) == []
         assert ctx.model(knot) == 0  # the failed calls kept no model
+        # per-model id and vertex-index arrays, one of them NULL: caller ids kept, the NULL entry numbered 0..n-1
+        ids_in = np.arange(1000, 1000 + knot.num_tris, dtype=np.int32)
+        vidx = np.ascontiguousarray(knot.faces, dtype=np.int32)
+        counts = np.array([knot.num_tris, knot.num_tris], dtype=np.int32)
+        id_ptrs = (C.c_void_p * 2)(ids_in.ctypes.data, None)
+        vidx_ptrs = (C.c_void_p * 2)(None, vidx.ctypes.data)
+        out = np.full(2, -1, dtype=np.int32)
+        assert lib.c2a_model_build_many(ctx.h, 2, api._ptr(counts), pp, C.cast(id_ptrs, C.c_void_p),
+                                        C.cast(vidx_ptrs, C.c_void_p), 2, api._ptr(out)) == api.OK
+        assert list(out) == [1, 2]
+        _, _, _, tid0, tidx0 = ctx.download(1)
+        _, _, _, tid1, tidx1 = ctx.download(2)
+        assert sorted(tid0) == list(ids_in) and sorted(tid1) == list(range(knot.num_tris))
+        assert (tidx0 == -1).all() and np.array_equal(np.sort(tidx1, axis=None), np.sort(vidx, axis=None))
+        assert np.array_equal(tid0 - 1000, tid1)  # the same tree
+
+
+@pytest.mark.parametrize("value", ["0", "-3", "many", "1", "64"])
+def test_build_threads_variable(lib, monkeypatch, value):
+    """C2A_BUILD_THREADS: a positive count caps the threads, anything else
+    means every hardware thread; the tree is the same either way."""
+    from c2a_gb300 import api, meshes
+
+    knot = meshes.torus_knot(2, 3, 200, 50)
+    monkeypatch.setenv("C2A_BUILD_THREADS", value)
+    with api.Context(-1) as ctx:
+        got = _model_digest(ctx, ctx.model(knot))
+    monkeypatch.setenv("C2A_BUILD_THREADS", "1")
+    with api.Context(-1) as ctx:
+        assert got == _model_digest(ctx, ctx.model(knot))
 
 
 def test_motion_matches_reference(lib):
