@@ -425,16 +425,20 @@ c2a_status c2a_launch_count(c2a_context *ctx, int64_t *count)
 
 namespace {
 
-/* host threads a build may use: C2A_BUILD_THREADS when set (>= 1), else every hardware thread */
+constexpr int kMaxBuildThreads = 256;
+
+/* host threads a build may use: the caller's count, else C2A_BUILD_THREADS
+ * when set (>= 1), else every hardware thread; at most kMaxBuildThreads */
 int build_thread_count(int32_t requested)
 {
-    if (requested > 0) return requested;
-    if (const char *e = getenv("C2A_BUILD_THREADS")) {
-        const int v = atoi(e);
-        if (v > 0) return v;
+    int n = requested;
+    if (n <= 0)
+        if (const char *e = getenv("C2A_BUILD_THREADS")) n = atoi(e);
+    if (n <= 0) {
+        const unsigned h = std::thread::hardware_concurrency();
+        n = h ? (int)h : 1;
     }
-    const unsigned h = std::thread::hardware_concurrency();
-    return h ? (int)h : 1;
+    return std::min(n, kMaxBuildThreads);
 }
 
 /* uploads a built model and adds it to the context's table (ctx->mu held) */

@@ -205,8 +205,8 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
 /* c2a_model_build over count models at once (the reference builds each
  * C2A_Model on its own, C2A/src/C2A_PQP.cpp:332-417): the models build on
  * parallel host threads, largest first, and a model's subtrees split over
- * the threads the others leave free.  threads: host threads to use, 0 for
- * C2A_BUILD_THREADS or else every hardware thread.  ids and vidx may be NULL,
+ * the threads the others leave free.  threads: host threads to use (at most
+ * 256), 0 for C2A_BUILD_THREADS or else every hardware thread.  ids and vidx may be NULL,
  * or hold NULL entries.  model_ids[i] is model i's id, in the order given;
  * every tree is bit-identical to a c2a_model_build of the same model.  On an
  * error no model of the call is kept. */
