@@ -465,7 +465,7 @@ c2a_status c2a_mlp_gemm(const uint16_t *A, const uint16_t *B, const float *bias,
     static bool attr[128] = {}; /* the shared-memory opt-in is a per-device attribute */
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return C2A_ERR_CUDA;
-    if (!encode) { /* the driver's tensor-map encoder, reached through the runtime */
+    if (!encode) { /* the CUDA driver API's tensor-map encoder, reached through the runtime */
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
