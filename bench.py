@@ -27,7 +27,9 @@ cpu_baseline: the oracle port on all host cores over a strided sample,
 compared with the GPU's results field by field and contact by contact.
 --impl reference: the CPU oracle port of the reference (bit-identical to
 the reference's own code) on all host cores, on a bounded sample, plus the
-same code on one core (cpu_baseline.single_core) over a smaller sample.
+same code on one core, one call per query, over a smaller sample
+(cpu_baseline.single_core: queries/s, latency mean/p50/p99/max, mean
+numCA and work counters per query).
 Under torchrun each rank runs its own replica batch (queries are independent).
 """
 from __future__ import annotations
@@ -182,6 +184,26 @@ def cpu_baseline(wl, idx, threads: int):
     return sub.n / dt, dt, res, con
 
 
+def cpu_latency(wl, idx):
+    """The oracle port on one core, each query of ``idx`` its own call: per-query
+    times (s) and results."""
+    from oracle.oracle import Port, build
+
+    build(ref=False)
+    port = Port()
+    models = port.models(wl.meshes)
+    sub = wl.subset(idx)
+    times = np.empty(sub.n)
+    parts = []
+    for k in range(sub.n):
+        t0 = time.perf_counter()
+        r, _ = port.solve_batch(models, sub.qint[k:k + 1], sub.poses[k:k + 1], sub.params, threads=1,
+                                contacts_per_query=CONTACT_SLOTS)
+        times[k] = time.perf_counter() - t0
+        parts.append(r)
+    return times, np.concatenate(parts)
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU oracle port of the reference on all host
     cores, over an evenly strided sample of the same batch (placed on the host)."""
@@ -200,11 +222,17 @@ def run_reference(args, rank, world):
         times.append(dt)
     value = float(wl.n * len(times) / sum(times))
     sample = f"{wl.n} of the {args.queries} queries, evenly strided, every step"
-    # the same code on one core, over every 16th query of that sample
+    # the same code on one core, one call per query, over every 16th query of that sample
     one_idx = all_idx[::16]
-    one_rate, one_dt, _, _ = cpu_baseline(wl, one_idx, 1)
-    single_core = {"value": one_rate, "unit": UNIT, "cores": 1,
-                   "sample": f"{len(one_idx)} of the {args.queries} queries, evenly strided, once ({one_dt:.1f} s)"}
+    lat, lres = cpu_latency(wl, one_idx)
+    single_core = {"value": float(len(lat) / lat.sum()), "unit": UNIT, "cores": 1,
+                   "sample": f"{len(one_idx)} of the {args.queries} queries, evenly strided, one call each "
+                             f"({lat.sum():.1f} s)",
+                   "latency_ms": {"mean": 1e3 * float(lat.mean()), "p50": 1e3 * float(np.percentile(lat, 50)),
+                                  "p99": 1e3 * float(np.percentile(lat, 99)), "max": 1e3 * float(lat.max())},
+                   "per_query_mean": {"numCA": float(lres["numCA"].mean()),
+                                      "num_bv_tests": float(lres["num_bv_tests"].mean()),
+                                      "num_tri_tests": float(lres["num_tri_tests"].mean())}}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
