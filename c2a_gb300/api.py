@@ -47,7 +47,7 @@ NOALLOC_MAX_MODELS = 120  # C2A_NOALLOC_MAX_MODELS
 
 # every extern "C" symbol of include/c2a_gb300.h
 ABI_SYMBOLS = ["c2a_create", "c2a_destroy", "c2a_status_str", "c2a_launch_count", "c2a_model_build",
-               "c2a_model_build_many", "c2a_model_info", "c2a_model_download", "c2a_model_download_obb", "c2a_model_free",
+               "c2a_model_build_many", "c2a_model_build_async", "c2a_model_wait", "c2a_model_info", "c2a_model_download", "c2a_model_download_obb", "c2a_model_free",
                "c2a_solve_batch",
                "c2a_solve_batch_device", "c2a_solve_batch_noalloc", "c2a_toc_step_batch", "c2a_contact_only_batch",
                "c2a_distance_batch", "c2a_solve_batch_hinted", "c2a_solve_batch_ordered",
@@ -117,6 +117,8 @@ def load(build_if_missing: bool = False) -> C.CDLL:
         "c2a_launch_count": ([vp, C.POINTER(C.c_int64)], i32),
         "c2a_model_build": ([vp, i32, vp, vp, vp, C.POINTER(i32)], i32),
         "c2a_model_build_many": ([vp, i32, vp, vp, vp, vp, i32, vp], i32),
+        "c2a_model_build_async": ([vp, i32, vp, vp, vp, C.POINTER(vp)], i32),
+        "c2a_model_wait": ([vp, C.POINTER(i32)], i32),
         "c2a_model_info": ([vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
         "c2a_model_download": ([vp, i32, vp, vp, vp, vp, vp], i32),
         "c2a_model_download_obb": ([vp, i32, vp], i32),
@@ -247,6 +249,22 @@ class Context:
                                              C.cast(vidx_ptrs, C.c_void_p), int(threads), _ptr(ids)),
                "c2a_model_build_many")
         return [int(i) for i in ids]
+
+    def model_async(self, mesh) -> "C.c_void_p":
+        """Starts building ``mesh`` on host threads (c2a_model_build_async); pass
+        the handle to model_wait for the id."""
+        tv = mesh.tri_verts()
+        vidx = np.ascontiguousarray(mesh.faces, dtype=np.int32)
+        h = C.c_void_p()
+        _check(self.lib.c2a_model_build_async(self.h, mesh.num_tris, _ptr(tv), None, _ptr(vidx), C.byref(h)),
+               "c2a_model_build_async")
+        return h
+
+    def model_wait(self, handle) -> int:
+        """Finishes an asynchronous build, uploads the model and returns its id."""
+        mid = C.c_int32()
+        _check(self.lib.c2a_model_wait(handle, C.byref(mid)), "c2a_model_wait")
+        return mid.value
 
     def model_info(self, mid: int) -> tuple[int, int, int]:
         a, b, c = C.c_int32(), C.c_int32(), C.c_int32()

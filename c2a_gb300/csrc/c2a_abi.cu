@@ -502,6 +502,62 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
     return register_model(ctx, slot, model_id);
 }
 
+struct c2a_build_handle {
+    c2a_context *ctx = nullptr;
+    std::vector<double> verts; /* copies of the caller's arrays */
+    std::vector<int32_t> ids, vidx;
+    ModelSlot slot;
+    int rc = 0;
+    std::thread worker;
+};
+
+c2a_status c2a_model_build_async(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
+                                 const int32_t *vidx, c2a_build_handle **handle)
+{
+    C2A_RANGE("c2a_model_build_async");
+    if (!ctx || !handle) return C2A_ERR_INVALID_ARGUMENT;
+    *handle = nullptr;
+    if (num_tris <= 0 || !tri_verts) return C2A_ERR_EMPTY_MODEL;
+    c2a_build_handle *h = new (std::nothrow) c2a_build_handle;
+    if (!h) return C2A_ERR_OUT_OF_MEMORY;
+    try {
+        h->ctx = ctx;
+        h->verts.assign(tri_verts, tri_verts + 9 * (size_t)num_tris);
+        if (ids) h->ids.assign(ids, ids + num_tris);
+        if (vidx) h->vidx.assign(vidx, vidx + 3 * (size_t)num_tris);
+        h->worker = std::thread([h, num_tris] {
+            BuildThreads threads(build_thread_count(0) - 1);
+            h->rc = build_rss_model(num_tris, h->verts.data(), h->ids.empty() ? nullptr : h->ids.data(),
+                                    h->vidx.empty() ? nullptr : h->vidx.data(), h->slot.host, &threads);
+        });
+    } catch (const std::exception &) { // no memory for the copies, or no thread
+        delete h;
+        return C2A_ERR_OUT_OF_MEMORY;
+    }
+    *handle = h;
+    return C2A_OK;
+}
+
+c2a_status c2a_model_wait(c2a_build_handle *handle, int32_t *model_id)
+{
+    C2A_RANGE("c2a_model_wait");
+    if (!handle) return C2A_ERR_INVALID_ARGUMENT;
+    handle->worker.join();
+    c2a_status s = handle->rc;
+    if (s == C2A_OK) {
+        int32_t id = -1;
+        {
+            std::lock_guard<std::mutex> lock(handle->ctx->mu);
+            s = register_model(handle->ctx, handle->slot, &id);
+        }
+        if (model_id) *model_id = s == C2A_OK ? id : -1;
+    } else if (model_id) {
+        *model_id = -1;
+    }
+    delete handle;
+    return s;
+}
+
 c2a_status c2a_model_build_many(c2a_context *ctx, int32_t count, const int32_t *num_tris,
                                 const double *const *tri_verts, const int32_t *const *ids,
                                 const int32_t *const *vidx, int32_t threads, int32_t *model_ids)

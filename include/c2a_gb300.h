@@ -213,6 +213,16 @@ c2a_status c2a_model_build(c2a_context *ctx, int32_t num_tris, const double *tri
 c2a_status c2a_model_build_many(c2a_context *ctx, int32_t count, const int32_t *num_tris,
                                 const double *const *tri_verts, const int32_t *const *ids,
                                 const int32_t *const *vidx, int32_t threads, int32_t *model_ids);
+/* c2a_model_build in two halves, so that a model builds on host threads
+ * while the GPU works on queries of the models already uploaded:
+ * c2a_model_build_async copies the arrays and returns at once with a handle;
+ * c2a_model_wait finishes the build, uploads the model, returns its id (or
+ * the build's error, -1 as the id) and frees the handle.  Every handle must
+ * be waited for once, before the context is destroyed. */
+typedef struct c2a_build_handle c2a_build_handle;
+c2a_status c2a_model_build_async(c2a_context *ctx, int32_t num_tris, const double *tri_verts, const int32_t *ids,
+                                 const int32_t *vidx, c2a_build_handle **handle);
+c2a_status c2a_model_wait(c2a_build_handle *handle, int32_t *model_id);
 c2a_status c2a_model_info(c2a_context *ctx, int32_t model_id, int32_t *num_tris, int32_t *num_nodes,
                           int32_t *depth);
 /* Host copy of the built hierarchy: node_f num_nodes x 25 doubles (R 9, Tr 3,

@@ -270,6 +270,29 @@ def test_build_many_rejects_bad_input_and_keeps_nothing(lib):
         assert np.array_equal(tid0 - 1000, tid1)  # the same tree
 
 
+def test_async_build_equals_build(lib):
+    """c2a_model_build_async + c2a_model_wait: the same tree as c2a_model_build,
+    ids in the order the waits register them, errors reported by the wait or
+    at once."""
+    import ctypes as C
+    from c2a_gb300 import api, meshes
+
+    ms = [meshes.torus_knot(2, 3, 400, 50), meshes.icosphere(3, noise=0.02, seed=3), meshes.triangle_soup(5000, seed=2)]
+    with api.Context(-1) as ctx:
+        want = [_model_digest(ctx, ctx.model(m)) for m in ms]
+    with api.Context(-1) as ctx:
+        handles = [ctx.model_async(m) for m in ms]  # all three build at once
+        ids = [ctx.model_wait(h) for h in reversed(handles)]
+        assert ids == [0, 1, 2]
+        assert [_model_digest(ctx, i) for i in reversed(ids)] == want
+        h = C.c_void_p()
+        assert lib.c2a_model_build_async(ctx.h, 0, None, None, None, C.byref(h)) == api.ERR_EMPTY_MODEL
+        assert not h.value
+        assert lib.c2a_model_build_async(ctx.h, 1, None, None, None, None) == api.ERR_INVALID_ARGUMENT
+        assert lib.c2a_model_wait(None, None) == api.ERR_INVALID_ARGUMENT
+        assert ctx.model(ms[1]) == 3
+
+
 @pytest.mark.parametrize("value", ["0", "-3", "many", "1", "64"])
 def test_build_threads_variable(lib, monkeypatch, value):
     """C2A_BUILD_THREADS: a positive count caps the threads, anything else
