@@ -200,3 +200,39 @@ def test_port_static_queries_match_reference_fixture(port):
         pairs, cbv, ctri = port.collide(models, a, b, z["R"][i], z["T"][i], 1)
         assert np.array_equal(pairs, z["pairs"][offs[i]:offs[i + 1]]), i
         assert (cbv, ctri) == tuple(z["collide_counts"][i]), i
+
+
+def _rel(RA, TA, RB, TB):
+    """B's pose in A's frame: R = RA^T RB, T = RA^T (TB - TA)."""
+    RA, RB = RA.reshape(3, 3), RB.reshape(3, 3)
+    return RA.T @ RB, RA.T @ (TB - TA)
+
+
+def test_toc_is_never_late_and_nothing_touches_earlier(port):
+    """The CA guarantee on config 1 (oracle = reference, bit for bit): where
+    the CA loop reached tolerance_d, the exact distance at the returned time
+    of contact is within th_ca and not negative, and at earlier times along
+    both motions (a quarter, half and three quarters of the TOC) the objects
+    are still apart."""
+    from c2a_gb300 import api, workloads
+
+    wl = workloads.config1(n=192, seed=7, device="cpu")
+    models = port.models(wl.meshes)
+    res, _ = port.solve_batch(models, wl.qint, wl.poses, wl.params, threads=4, contacts_per_query=0)
+    hit = np.flatnonzero((res["collisionfree"] == 0) & (res["distance"] <= wl.params["tol_d"]) &
+                         (res["numCA"] >= 2) & (res["distance"] > 0))
+    assert len(hit) >= 10
+    th = wl.params["th_ca"]
+    for q in hit:
+        r = res[q]
+        R, T = _rel(r["R_toc"][0], r["T_toc"][0], r["R_toc"][1], r["T_toc"][1])
+        d, _, _ = port.distance(models, 0, 0, R, T, int(r["seed_a"]), int(r["seed_b"]))
+        assert 0 <= d <= th * (1 + 1e-12), (q, d, th)
+        P = wl.poses[q]
+        for frac in (0.25, 0.5, 0.75):
+            t = frac * float(r["toc"])
+            RA, TA, _ = api.motion_integrate(P[0:9], P[9:12], P[12:21], P[21:24], t)
+            RB, TB, _ = api.motion_integrate(P[24:33], P[33:36], P[36:45], P[45:48], t)
+            R, T = _rel(RA, TA, RB, TB)
+            d_early, _, _ = port.distance(models, 0, 0, R, T, 0, 0)
+            assert d_early > 0, (q, frac, d_early)
