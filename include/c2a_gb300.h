@@ -9,6 +9,9 @@
  *                            (C2A/src/C2A_PQP.cpp:82-417) with the RSS
  *                            hierarchy build of C2A_BuildModel
  *                            (C2A/src/C2A_Build.cpp:546-574)
+ *   c2a_model_build_many,    the same EndModel for many models at once, or
+ *   c2a_model_build_async,   in two halves (the build on host threads, then
+ *   c2a_model_wait           the upload)
  *   c2a_solve_batch          C2A_Solve (C2A/C2A.h:23-35, C2A/src/C2A.cpp:2315)
  *                            over many independent queries; each query is
  *                            C2A_QueryTimeOfContact (C2A/C2A.h:274-281)
