@@ -591,8 +591,8 @@ c2a_status c2a_model_build_many(c2a_context *ctx, int32_t count, const int32_t *
     for (int w = 1; w < workers; w++) {
         try {
             pool.emplace_back(work);
-        } catch (const std::system_error &) {
-            break; // fewer workers; the ones running take the rest
+        } catch (const std::exception &) { // no thread (system_error) or no room to keep it
+            break;                          // fewer workers; the ones running take the rest
         }
     }
     work();
