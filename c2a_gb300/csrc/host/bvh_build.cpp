@@ -521,13 +521,13 @@ constexpr int64_t kPartMin = 16384;     /* records a thread of such a pass handl
  * thread, the others on threads taken from the budget (given back after) */
 template <class Body> void parallel_parts(int64_t n, BuildThreads *threads, Body body)
 {
+    std::vector<std::thread> pool;
+    std::vector<int> here; // parts no thread could be started for
+    pool.reserve(kMaxParts);
+    here.reserve(kMaxParts);
     int extra = 0;
     while (threads && extra + 1 < kMaxParts && (int64_t)(extra + 2) * kPartMin <= n && threads->take()) extra++;
     const int parts = extra + 1;
-    std::vector<std::thread> pool;
-    std::vector<int> here; // parts no thread could be started for
-    pool.reserve(parts);
-    here.reserve(parts);
     for (int p = 1; p < parts; p++) {
         const int64_t lo = n * p / parts, hi = n * (p + 1) / parts;
         try {
