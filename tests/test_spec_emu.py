@@ -18,10 +18,11 @@ WARP, SPEC = 1, 4
 SLOTS = 512
 
 
-def _build_emu(tmp_path_factory, name, defines=()):
+def _build_emu(tmp_path_factory, name, defines=(), flags=()):
     out = str(tmp_path_factory.mktemp(name) / f"lib{name}.so")
     subprocess.run(["g++", "-std=c++20", "-O1", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
-                    "-w", *[f"-D{d}" for d in defines], "-o", out, os.path.join(ROOT, "tests", "cpp", "spec_emu.cpp"),
+                    "-w", *flags, *[f"-D{d}" for d in defines], "-o", out,
+                    os.path.join(ROOT, "tests", "cpp", "spec_emu.cpp"),
                     os.path.join(ROOT, "c2a_gb300", "csrc", "host", "bvh_build.cpp")], check=True)
     return out
 
@@ -105,3 +106,41 @@ def test_emulated_filtered_warp_engine_matches_fixture(emu_filter, name):
     offs = np.concatenate([[0], np.cumsum([min(SLOTS, off[i + 1] - off[i]) for i in sel])])
     bad = result_mismatches(res, exp[sel], con, flat, offs)
     assert not bad, describe(res, exp[sel], bad[0])
+
+
+def test_emulated_engines_under_address_sanitizer(tmp_path_factory):
+    """The warp and speculative engines' device source on the host emulator,
+    built with AddressSanitizer + UBSan and run in a child process with the
+    sanitizer runtime preloaded: fixture queries run without a report and
+    give the reference's bits."""
+    import sys
+
+    asan = subprocess.run(["g++", "-print-file-name=libasan.so"], capture_output=True, text=True).stdout.strip()
+    if not os.path.isabs(asan) or not os.path.exists(asan):
+        pytest.skip("no AddressSanitizer runtime")
+    lib = _build_emu(tmp_path_factory, "emu_asan",
+                     flags=("-g", "-fno-omit-frame-pointer", "-fsanitize=address,undefined", "-fno-sanitize-recover=all"))
+    tests_dir = os.path.join(ROOT, "tests")
+    script = f"""
+import ctypes as C, sys
+import numpy as np
+sys.path[:0] = [{tests_dir!r}, {ROOT!r}]
+import test_spec_emu as t
+from c2a_testutil import load_fixture, result_mismatches
+lib = C.CDLL({lib!r})
+lib.spec_emu_model.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+lib.spec_emu_solve.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double]
+for name in ("mixed", "translation"):
+    ms, qint, poses, params, exp, econ, off = load_fixture(name)
+    sel = np.linspace(0, len(qint) - 1, 4).astype(int)
+    flat = np.concatenate([econ[off[i]:off[i + 1]][:t.SLOTS] for i in sel])
+    offs = np.concatenate([[0], np.cumsum([min(t.SLOTS, off[i + 1] - off[i]) for i in sel])])
+    for engine in (t.WARP, t.SPEC):
+        res, con = t._run(lib, ms, qint[sel], poses[sel], params, engine)
+        assert not result_mismatches(res, exp[sel], con, flat, offs), (name, engine)
+print("clean")
+"""
+    env = dict(os.environ, LD_PRELOAD=asan, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1",
+               UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1")
+    r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=1200)
+    assert r.returncode == 0 and "clean" in r.stdout, r.stdout[-2000:] + r.stderr[-6000:]
